@@ -1,0 +1,221 @@
+/*
+ * ttg.h -- C ABI of the GB300 (sm_103a) Chebyshev-filtered subspace
+ * iteration library (libttg.so).
+ *
+ * Plain C types only: pointers, sizes, doubles.  Every entry point returns a
+ * ttg_status; nothing terminates the process.  One CUDA stream per ttg_op;
+ * calls on one handle are not thread-safe, calls on different handles are.
+ * Entry points that return data in host memory synchronise the op's stream;
+ * the others only enqueue work.
+ *
+ * Layout conventions (those of the reference's PETSc dense Mats):
+ *   - a vector block X is N x k, column-major (one column per state), ld >= N;
+ *   - k x k matrices (overlap, projected H, eigenvectors) are column-major;
+ *   - CSR matrices use int64 row pointers and int32 column indices.
+ * Inside the library, blocks live in HBM row-major (one row per basis index)
+ * so that a row of X is one contiguous, vector-loadable segment.
+ */
+#ifndef TTG_H_
+#define TTG_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TTG_OK = 0,
+  TTG_BAD_ARG = 1,     /* null pointer, size out of range, mismatched shapes */
+  TTG_BAD_CSR = 2,     /* row pointers not monotone, column out of range, ... */
+  TTG_OOM = 3,         /* device allocation failed */
+  TTG_NOT_SPD = 4,     /* Cholesky met a non-positive pivot */
+  TTG_NONFINITE = 5,   /* NaN/Inf found in an input or an intermediate */
+  TTG_TIMEOUT = 6,     /* a bounded device-side wait ran out */
+  TTG_CUDA_ERR = 7,    /* a CUDA runtime call failed */
+  TTG_NO_DEVICE = 8,   /* no usable sm_100+ device */
+  TTG_NOT_CONVERGED = 9 /* an iteration hit its limit (eigensolver, Fermi) */
+} ttg_status;
+
+typedef enum {
+  TTG_PREC_FP64 = 0,   /* H and the block in FP64, FP64 accumulation */
+  TTG_PREC_FP32 = 1,   /* H and the block in FP32, FP32 accumulation */
+  TTG_PREC_BF16 = 2    /* H and the block stored in BF16, FP32 accumulation */
+} ttg_prec;
+
+/* Precision schedule of one Chebyshev filter call: the first `n_low` degrees
+ * run in `low`, the remaining ones in `high`.  `return_prev` = 1 reproduces
+ * the reference exactly: its filter hands back the degree m-1 iterate
+ * (eigensolver/ChebyShevFilter.cc:163-176), which this library computes
+ * with m-1 operator applications; 0 returns the degree-m iterate. */
+typedef struct {
+  int32_t low;
+  int32_t high;
+  int32_t n_low;
+  int32_t return_prev;
+} ttg_sched;
+
+typedef struct ttg_op ttg_op;        /* device-resident operator + workspace */
+typedef struct ttg_block ttg_block;  /* device-resident N x k FP64 block */
+
+typedef struct {
+  int64_t n;              /* rows of H_loc */
+  int64_t nnz_h;          /* nonzeros of H_loc */
+  int64_t nnz_c;          /* nonzeros of C */
+  int32_t nproj;          /* projector rows of C */
+  int32_t group_rows;     /* rows per row group of the device format */
+  int64_t n_groups;
+  int64_t stored_cols;    /* merged column slots over all groups */
+  double fill;            /* (nnz_h + nnz_c^T) / (group_rows * stored_cols) */
+  int64_t device_bytes;   /* HBM held by the operator */
+  int64_t launches;       /* kernels this op has launched so far */
+} ttg_op_info_t;
+
+/* ---- device and operator ------------------------------------------------ */
+
+/* Library version string and the device it would use. */
+const char* ttg_version(void);
+ttg_status ttg_device_query(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
+const char* ttg_status_string(ttg_status s);
+
+/* Upload the projected Hamiltonian.  Replaces AX::AX + AX::setup_system +
+ * AX::setup_mata_on_device (eigensolver/Mult.h:37-44,
+ * eigensolver/MultCuda.cu:38-371), which copy H_loc to the device, and
+ * takes the nonlocal part that ChebyShevFilter applies with PETSc on the host
+ * (eigensolver/ChebyShevFilter.cc:103-124; matrices from
+ * dft/ProjectHamiltonianSparse.h:97): C (nproj x n) and D (nproj) such that
+ * C_nloc = diag(D) C and C_nloc_trans = C^T.  nproj may be 0.
+ * max_k bounds the block width used with this op.  The CSR is validated on
+ * the host before anything is launched (TTG_BAD_CSR). */
+ttg_status ttg_op_create(int64_t n, const int64_t* h_row_ptr, const int32_t* h_col,
+                         const double* h_val, int32_t nproj, const int64_t* c_row_ptr,
+                         const int32_t* c_col, const double* c_val, const double* d,
+                         int32_t max_k, ttg_op** out);
+/* Replaces AX::free_mata_on_device / AX::~AX (eigensolver/MultCuda.cu:673-717). */
+ttg_status ttg_op_destroy(ttg_op* op);
+ttg_status ttg_op_info(const ttg_op* op, ttg_op_info_t* info);
+/* The op's cudaStream_t, as an opaque pointer, for callers that overlap work. */
+void* ttg_op_stream(ttg_op* op);
+ttg_status ttg_op_sync(ttg_op* op);
+/* Device-side timing on the op's stream (slot 0..15). */
+ttg_status ttg_op_record(ttg_op* op, int32_t slot);
+ttg_status ttg_op_elapsed_ms(ttg_op* op, int32_t slot0, int32_t slot1, float* ms);
+
+/* ---- vector blocks (the reference's dense Mat X, N x k) ----------------- */
+
+ttg_status ttg_block_create(ttg_op* op, int32_t k, ttg_block** out);
+ttg_status ttg_block_destroy(ttg_block* b);
+int32_t ttg_block_cols(const ttg_block* b);
+/* Host <-> device, column-major N x k with leading dimension ld. */
+ttg_status ttg_block_set(ttg_block* b, const double* x_colmajor, int64_t ld);
+ttg_status ttg_block_get(ttg_block* b, double* x_colmajor, int64_t ld);
+/* Device-pointer variants (no host copy); column-major, ld >= N. */
+ttg_status ttg_block_set_device(ttg_block* b, const double* x_colmajor_dev, int64_t ld);
+ttg_status ttg_block_get_device(ttg_block* b, double* x_colmajor_dev, int64_t ld);
+ttg_status ttg_block_copy(ttg_block* dst, const ttg_block* src);
+
+/* ---- the hot path --------------------------------------------------------- */
+
+/* Chebyshev filter, in place on X.  Replaces
+ * ChebyShevFilter::computeFilteredSubspace (eigensolver/ChebyShevFilter.h:31-39,
+ * eigensolver/ChebyShevFilter.cc:34-189): a = lower bound of the unwanted
+ * spectrum, b = upper bound, a0 = lowest wanted eigenvalue, m = degree.
+ * Each degree is one fused launch: Ynew = alpha*(H_loc Y + C^T D C Y)
+ * + beta*Y + delta*X.  num_x_blocks of the reference only splits the columns
+ * to bound host memory; here the whole block is filtered at once. */
+ttg_status ttg_cheb_filter(ttg_op* op, ttg_block* X, int32_t m, double a, double b,
+                           double a0, ttg_sched sched);
+
+/* HX = (H_loc + C^T D C) X in FP64.  Replaces AX::perform_ax
+ * (eigensolver/Mult.h:46-53, eigensolver/MultCuda.cu:719-820) plus the
+ * nonlocal MatMatMults of main.cc:1066-1092. */
+ttg_status ttg_apply_h(ttg_op* op, const ttg_block* X, ttg_block* HX);
+
+/* S = X^T Y (k x k, column-major), FP64.  Replaces MultTM::mult
+ * (eigensolver/MultTm.h:37, eigensolver/MultTm.cu:86-224).  s_host may be
+ * NULL when only the device copy is wanted (kept inside the op). */
+ttg_status ttg_gram(ttg_op* op, const ttg_block* X, const ttg_block* Y, double* s_host);
+
+/* Cholesky-QR in FP64: S = X^T X = L L^T, X <- X L^-T.  Replaces MultTM::orth
+ * (eigensolver/MultTm.h:39, eigensolver/MultTm.cu:226-467).  Returns
+ * TTG_NOT_SPD (X untouched) when S is not numerically positive definite. */
+ttg_status ttg_chol_qr(ttg_op* op, ttg_block* X);
+
+/* Symmetric eigendecomposition of a k x k column-major FP64 matrix, ascending
+ * eigenvalues, eigenvectors as columns.  Replaces
+ * EigenSolver::computeEigenPairsSeq (eigensolver/EigenSolver.h:32-38,
+ * eigensolver/EigenSolver.cc:30-184).  Host in/out; the work runs on the GPU. */
+ttg_status ttg_syev(ttg_op* op, int32_t k, const double* a_host, double* w_host,
+                    double* v_host);
+
+/* Rayleigh-Ritz on X: HX = H X, P = X^T HX, P = Q diag(w) Q^T; if rotate != 0
+ * also X <- X Q.  main.cc:1066-1115 (projection + eig) and main.cc:1186-1207
+ * (rotation).  w_host (k) and q_host (k x k) may be NULL. */
+ttg_status ttg_rayleigh_ritz(ttg_op* op, ttg_block* X, int32_t rotate, double* w_host,
+                             double* q_host);
+
+/* X <- X Q with Q k x k column-major on the host.  main.cc:1186-1207. */
+ttg_status ttg_rotate(ttg_op* op, ttg_block* X, const double* q_host);
+
+/* Lanczos spectral bounds with (H_loc + C^T D C).  Replaces
+ * EigenSolver::computeUpperBoundWithLanczos (eigensolver/EigenSolver.h:40-44,
+ * eigensolver/EigenSolver.cc:186-388): upper = |lambda_max(T)| + ||f||,
+ * lower = lambda_min(T).  v0 (length n) is the start vector; the reference
+ * draws it with VecSetRandom. */
+ttg_status ttg_lanczos_bounds(ttg_op* op, const double* v0_host, int32_t max_iter,
+                              double* upper, double* lower);
+
+/* One ChFSI pass as main.cc:1047-1115 runs it: filter, Cholesky-QR,
+ * Rayleigh-Ritz (eigenvalues to w_host, optional), and, if rotate != 0,
+ * the rotation X <- X Q. */
+ttg_status ttg_chfsi_pass(ttg_op* op, ttg_block* X, int32_t m, double a, double b,
+                          double a0, ttg_sched sched, int32_t rotate, double* w_host);
+
+/* ---- Fermi level, density, Hartree --------------------------------------- */
+
+/* Fermi level by Newton on sum_i 2 f_i = n_electrons and the occupations f_i.
+ * Replaces KSDFTEnergyFunctional::computeFermiEnergy
+ * (dft/KSDFTEnergyFunctional.cc:76-124) and the occupancy loop of
+ * main.cc:1239-1272.  kT = kb*T in Ha.  Runs in FP64 on the GPU. */
+ttg_status ttg_fermi(ttg_op* op, int32_t k, const double* eig_host, double n_electrons,
+                     double kT, int32_t max_iter, double* mu, double* occ_host);
+
+/* Nodal density rho(x,y,z) = sum_i 2 f_i (c_i x1 Ux x2 Uy x3 Uz)^2 where c_i
+ * is column i of X (an rx*ry*rz Tucker core, x fastest) and Ux (nx x rx),
+ * Uy, Uz (column-major) are the basis values at the nodes.  Output is
+ * nx*ny*nz, x fastest, host memory.  Replaces the per-state reconstruction of
+ * ProjectHamiltonianSparse::computeRhoOut (dft/ProjectHamiltonianSparse.cc:
+ * 1021-1075).  FP32 tensor-core mode products with a 3-term TF32 split,
+ * FP32 accumulation of rho. */
+ttg_status ttg_density(ttg_op* op, const ttg_block* X, const double* occ_host,
+                       int32_t rx, int32_t ry, int32_t rz,
+                       int32_t nx, int32_t ny, int32_t nz,
+                       const double* ux, const double* uy, const double* uz,
+                       double* rho_host);
+
+/* Hartree potential by the Gaussian kernel expansion
+ *   V(i,j,l) = sum_t w_t sum_abc G_abc Fx_t[i,a] Fy_t[j,b] Fz_t[l,c]
+ *   Fx_t[i,a] = sum_q wq_q exp(-alpha_t (x_i - xq_q)^2) Ux[q,a]
+ * (dft/KSDFTPotential.cc:269-340, factor integrals :440-599, per-term
+ * contraction :601-658).  G is rx*ry*rz (x fastest); Ux is nqx x rx
+ * column-major values of the density's Tucker factors at the quadrature
+ * points xq with weights wq (J*w); the target grid is x (nx points).
+ * alpha and omega are the already-scaled expansion coefficients.
+ * All K terms run in one persistent launch on the tensor cores with a 3-term
+ * TF32 split (FP32 accuracy); output nx*ny*nz, x fastest, host memory.
+ * Needs no op (creates its own stream); device memory is released on return. */
+ttg_status ttg_hartree(int32_t K, const double* alpha, const double* omega,
+                       int32_t rx, int32_t ry, int32_t rz, const double* G,
+                       int32_t nqx, int32_t nqy, int32_t nqz,
+                       const double* xq, const double* yq, const double* zq,
+                       const double* wqx, const double* wqy, const double* wqz,
+                       const double* ux, const double* uy, const double* uz,
+                       int32_t nx, int32_t ny, int32_t nz,
+                       const double* x, const double* y, const double* z,
+                       double* v_host, float* kernel_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TTG_H_ */

@@ -1,0 +1,294 @@
+"""GPU parity: every libttg entry point against the FP64 oracle on the same
+seeded inputs, through the C ABI.  Tolerances are stated per test:
+  FP64 paths    ~1e-11 relative (summation order only)
+  FP32 filter   1e-5 relative to the block's max entry
+  BF16 degrees  checked through the Ritz values they lead to
+  eigenvalues   1e-6 Ha after convergence (the method's acceptance bound)
+"""
+import os
+import struct
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from ttdft_public_gb300 import api, system
+from ttdft_public_gb300._lib import TtgError
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def dense_h(s):
+    C = s.C.to_dense()
+    return s.H.to_dense() + C.T @ np.diag(s.D) @ C
+
+
+@pytest.fixture(scope="module")
+def tiny_op(tiny_system):
+    op = api.Operator(api.ProjectHamiltonianSparse.from_system(tiny_system), 32)
+    yield op
+    op.close()
+
+
+@pytest.fixture(scope="module")
+def small_op(small_system):
+    op = api.Operator(api.ProjectHamiltonianSparse.from_system(small_system), 64)
+    yield op
+    op.close()
+
+
+def bounds(s, k):
+    w = np.linalg.eigvalsh(dense_h(s))
+    return w, w[k + 4], w[-1] * 1.02, w[0]
+
+
+def test_op_info_counts_nonzeros(tiny_op, tiny_system):
+    inf = tiny_op.info()
+    assert inf["n"] == tiny_system.N
+    assert inf["nnz_h"] == tiny_system.H.nnz
+    assert inf["nnz_c"] == tiny_system.C.nnz
+    assert 0 < inf["fill"] <= 1.0
+
+
+def test_block_roundtrip(tiny_op, tiny_system):
+    X = np.random.default_rng(0).standard_normal((tiny_system.N, 7))
+    B = api.Mat(tiny_op, 7, X)
+    assert np.array_equal(B.get(), X)
+
+
+@pytest.mark.parametrize("k", [1, 5, 16])
+def test_apply_h_fp64(tiny_op, tiny_system, k):
+    X = np.random.default_rng(k).standard_normal((tiny_system.N, k))
+    ax = api.AX(1, k)
+    ax.op = tiny_op
+    Xm, Ym = api.Mat(tiny_op, k, X), api.Mat(tiny_op, k)
+    ax.perform_ax(Xm, Ym)
+    assert rel(Ym.get(), oracle.apply_h(tiny_system, X)) < 1e-12
+
+
+@pytest.mark.parametrize("return_prev", [False, True])
+@pytest.mark.parametrize("k", [6, 24])
+def test_filter_fp64_matches_oracle(small_op, small_system, return_prev, k):
+    s = small_system
+    w, a, b, a0 = bounds(s, k)
+    X = np.random.default_rng(10 + k).standard_normal((s.N, k))
+    Xm = api.Mat(small_op, k, X)
+    f = api.ChebyShevFilter(api.sched("fp64", return_prev=return_prev))
+    ax = api.AX(1, k)
+    ax.op = small_op
+    f.computeFilteredSubspace(None, ax, Xm, s.N, 12, a, b, a0)
+    ref = oracle.cheb_filter(s, X, 12, a, b, a0, return_prev=return_prev)
+    assert rel(Xm.get(), ref) < 1e-11
+
+
+@pytest.mark.parametrize("k", [8, 24, 36])
+def test_filter_fp32_matches_oracle(small_op, small_system, k):
+    s = small_system
+    w, a, b, a0 = bounds(s, k)
+    X = np.random.default_rng(20 + k).standard_normal((s.N, k))
+    Xm = api.Mat(small_op, k, X)
+    ax = api.AX(1, k)
+    ax.op = small_op
+    api.ChebyShevFilter(api.sched("fp32")).computeFilteredSubspace(None, ax, Xm, s.N, 12, a, b, a0)
+    ref = oracle.cheb_filter(s, X, 12, a, b, a0)
+    assert rel(Xm.get(), ref) < 1e-5
+
+
+def test_filter_degree_one_reference_returns_input(small_op, small_system):
+    X = np.random.default_rng(3).standard_normal((small_system.N, 4))
+    Xm = api.Mat(small_op, 4, X)
+    ax = api.AX(1, 4)
+    ax.op = small_op
+    api.ChebyShevFilter(api.sched("fp64", return_prev=True)).computeFilteredSubspace(
+        None, ax, Xm, small_system.N, 1, 0.5, 5.0, 0.1)
+    assert np.array_equal(Xm.get(), X)
+
+
+def test_gram_and_cholqr(small_op, small_system):
+    rng = np.random.default_rng(4)
+    X = rng.standard_normal((small_system.N, 40))
+    Y = rng.standard_normal((small_system.N, 40))
+    Xm, Ym = api.Mat(small_op, 40, X), api.Mat(small_op, 40, Y)
+    mt = api.MultTM()
+    assert rel(mt.mult(Xm, Ym), X.T @ Y) < 1e-13
+    mt.orth(Xm)
+    Q = Xm.get()
+    ref, st = oracle.cholqr(X)
+    assert st == 0
+    assert rel(Q, ref) < 1e-11
+    assert np.abs(Q.T @ Q - np.eye(40)).max() < 1e-12
+
+
+def test_cholqr_not_spd_is_reported_and_x_untouched(small_op, small_system):
+    X = np.random.default_rng(5).standard_normal((small_system.N, 8))
+    X[:, 6] = X[:, 2]
+    Xm = api.Mat(small_op, 8, X)
+    with pytest.raises(TtgError) as e:
+        api.MultTM().orth(Xm)
+    assert e.value.status == "NOT_SPD"
+    assert np.array_equal(Xm.get(), X)
+
+
+@pytest.mark.parametrize("k", [3, 20, 64, 161])
+def test_syev_matches_lapack(k):
+    s = system.build_system(system.small_spec())
+    op = api.Operator(api.ProjectHamiltonianSparse.from_system(s), 200)
+    rng = np.random.default_rng(k)
+    A = rng.standard_normal((k, k))
+    A = A + A.T
+    w = np.zeros(k)
+    V = np.zeros((k, k), order="F")
+    api.EigenSolver(op).computeEigenPairsSeq(A, k, k, w, V)
+    wr, Vr = oracle.eigh(A)
+    assert np.abs(w - wr).max() < 1e-12 * np.abs(wr).max()
+    assert np.abs(np.abs(V.T @ Vr) - np.eye(k)).max() < 1e-9
+    assert np.abs(A @ V - V * w).max() < 1e-11 * np.abs(wr).max()
+    op.close()
+
+
+def test_lanczos_bounds_match_oracle(small_op, small_system):
+    v0 = np.random.default_rng(6).uniform(0, 1, small_system.N)
+    up, lo = api.EigenSolver(small_op).computeUpperBoundWithLanczos(None, 20, v0=v0)
+    rup, rlo = oracle.lanczos_bounds(small_system, v0, 20)
+    assert abs(up - rup) < 1e-9 * abs(rup)
+    assert abs(lo - rlo) < 1e-9 * max(1.0, abs(rlo))
+
+
+def test_rayleigh_ritz_matches_oracle(small_op, small_system):
+    s = small_system
+    X, _ = oracle.cholqr(np.random.default_rng(7).standard_normal((s.N, 24)))
+    Xm = api.Mat(small_op, 24, X)
+    w = api.rayleigh_ritz(small_op, Xm, rotate=True)
+    wr, Q, Xr = oracle.rayleigh_ritz(s, X)
+    assert np.abs(w - wr).max() < 1e-11 * np.abs(wr).max()
+    # rotated block: compare column by column up to sign
+    Xg = Xm.get()
+    dots = np.abs(np.sum(Xg * Xr, axis=0)) / (np.linalg.norm(Xg, axis=0) * np.linalg.norm(Xr, axis=0))
+    assert np.all(dots > 1 - 1e-9)
+
+
+def chfsi_converge(op, s, k, m, sch, passes, seed=8):
+    """main.cc:987-1207 restart loop, GPU path."""
+    v0 = np.random.default_rng(seed).uniform(0, 1, s.N)
+    upper, lower = api.EigenSolver(op).computeUpperBoundWithLanczos(None, 20, v0=v0)
+    X = np.random.default_rng(seed + 1).standard_normal((s.N, k))
+    Xm = api.Mat(op, k, X)
+    a, a0 = 0.0, lower
+    w = None
+    for _ in range(passes):
+        w = api.chfsi_pass(op, Xm, m, a, upper, a0, sch, rotate=True)
+        a0, a = w[0], w[-1]
+    return w, Xm
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp32", "mixed"])
+def test_chfsi_converges_to_exact_eigenvalues(small_op, small_system, mode):
+    s = small_system
+    k, m, nocc = 24, 12, 16
+    sch = {"fp64": api.sched("fp64"), "fp32": api.sched("fp32"),
+           "mixed": api.sched("fp32", low="bf16", n_low=4)}[mode]
+    w, _ = chfsi_converge(small_op, s, k, m, sch, passes=25)
+    exact = np.linalg.eigvalsh(dense_h(s))[:k]
+    # acceptance: eigenvalues within 1e-6 Ha of the FP64 answer (occupied part)
+    assert np.abs(w[:nocc] - exact[:nocc]).max() < 1e-6
+
+
+def test_fermi_matches_oracle(small_op):
+    eig = np.sort(np.random.default_rng(9).uniform(-1, 1, 64))
+    kT = 3.166811429e-6 * 500.0
+    mu, occ = api.fermi(small_op, eig, 40, kT)
+    rmu, rocc = oracle.fermi(eig, 40, kT)
+    assert abs(mu - rmu) < 1e-12
+    assert np.abs(occ - rocc).max() < 1e-12
+
+
+def test_density_matches_oracle(small_op, small_system):
+    s = small_system
+    X, _ = oracle.cholqr(np.random.default_rng(10).standard_normal((s.N, 24)))
+    occ = np.linspace(1.0, 0.0, 24)
+    rho = api.density(small_op, api.Mat(small_op, 24, X), occ, s.basis)
+    ref = oracle.density(X, occ, s.basis)
+    # FP32 tensor-core mode products (3-term TF32 split), FP32 accumulation
+    assert np.linalg.norm(rho - ref) / np.linalg.norm(ref) < 1e-6
+
+
+def hartree_case(seed=0, r=(12, 10, 8), nq=(40, 36, 30), n=(33, 31, 29), K=7):
+    rng = np.random.default_rng(seed)
+    G = rng.standard_normal((r[2], r[1], r[0]))
+    quad, U, grids = [], [], []
+    for d in range(3):
+        xq = np.sort(rng.uniform(0, 10, nq[d]))
+        wq = rng.uniform(0.1, 0.3, nq[d])
+        quad.append((xq, wq))
+        U.append(rng.standard_normal((nq[d], r[d])))
+        grids.append(np.linspace(0, 10, n[d]))
+    alpha = np.geomspace(1e-3, 30.0, K)
+    omega = rng.uniform(0.1, 1.0, K)
+    return alpha, omega, G, quad, U, grids
+
+
+def test_hartree_matches_oracle():
+    args = hartree_case()
+    V, ms = api.hartree(*args)
+    ref = oracle.hartree(*args)
+    assert np.linalg.norm(V - ref) / np.linalg.norm(ref) < 1e-6
+
+
+def write_driver_input(path, s, k, m, passes, X0, a_init=0.0, lanczos=20):
+    H, C = s.H, s.C
+    with open(path, "wb") as f:
+        f.write(struct.pack("<8q", s.N, H.nnz, C.n_rows, C.nnz, k, m, passes, lanczos))
+        f.write(struct.pack("<d", a_init))
+        for arr, dt in ((H.row_ptr, np.int64), (H.col, np.int32), (H.val, np.float64),
+                        (C.row_ptr, np.int64), (C.col, np.int32), (C.val, np.float64),
+                        (s.D, np.float64)):
+            f.write(np.ascontiguousarray(arr, dt).tobytes())
+        f.write(np.asfortranarray(X0).tobytes(order="F"))
+
+
+def test_cxx_driver_matches_python_api(small_system, tmp_path):
+    """The reference-shaped C++ classes (AX, ChebyShevFilter, MultTM,
+    EigenSolver) reproduce the oracle's ChFSI loop."""
+    from ttdft_public_gb300 import build
+    exe = build.build_driver()
+    s = small_system
+    k, m, passes = 24, 10, 6
+    X0 = np.random.default_rng(11).standard_normal((s.N, k))
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    write_driver_input(inp, s, k, m, passes, X0)
+    r = subprocess.run([exe, str(inp), str(out), "fp64"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    res = np.fromfile(out, dtype=np.float64)
+    upper, lower, w = res[0], res[1], res[2:2 + k]
+    # oracle loop with the driver's Lanczos bounds (its start vector is its own)
+    X = X0.copy()
+    a, a0 = 0.0, lower
+    for _ in range(passes):
+        X = oracle.cheb_filter(s, X, m, a, upper, a0, return_prev=True)
+        X, st = oracle.cholqr(X)
+        wr, Q, _ = oracle.rayleigh_ritz(s, X, rotate_x=False)
+        a0, a = wr[0], wr[-1]
+    assert np.abs(w - wr).max() < 1e-9 * np.abs(wr).max()
+
+
+def test_bad_csr_rejected_before_launch(tiny_system):
+    s = tiny_system
+    bad_col = s.H.col.copy()
+    bad_col[5] = s.N + 3
+    H = system.Csr(s.N, s.N, s.H.row_ptr, bad_col, s.H.val)
+    with pytest.raises(TtgError) as e:
+        api.Operator(api.ProjectHamiltonianSparse(H), 8)
+    assert e.value.status == "BAD_CSR"
+
+
+def test_nonfinite_block_rejected(tiny_op, tiny_system):
+    X = np.ones((tiny_system.N, 3))
+    X[7, 1] = np.nan
+    with pytest.raises(TtgError) as e:
+        api.Mat(tiny_op, 3, X)
+    assert e.value.status == "NONFINITE"

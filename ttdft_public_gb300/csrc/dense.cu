@@ -1,0 +1,537 @@
+// FP64 dense kernels of the Rayleigh-Ritz step.
+//
+//   gram_tn        S = X^T Y (k x k), split over rows with a fixed-order
+//                  reduction of the partial tiles (bitwise reproducible).
+//                  MultTM::mult, eigensolver/MultTm.cu:86-224.
+//   gemm_nn_small  out = X Q or X Q^T, Q k x k.  Subspace rotation
+//                  (main.cc:1186-1207) and the X L^-T of Cholesky-QR
+//                  (eigensolver/MultTm.cu:422-438 / the SOLVE_WITH_INVERSE
+//                  variant :309-404).
+//   cholesky_inv   S = L L^T and L^-1, status on a non-positive pivot
+//                  (the reference ignores potrf's info, MultTm.cu:283-294).
+//   syev_jacobi    symmetric eigensolver (cyclic Jacobi, round-robin pair
+//                  ordering, all disjoint rotations of a round in parallel),
+//                  ascending eigenvalues; replaces the SLEPc/LAPACK call of
+//                  EigenSolver::computeEigenPairsSeq (EigenSolver.cc:30-184).
+//   lanczos_step   one Lanczos three-term step on the device
+//                  (EigenSolver.cc:262-315).
+//   fermi          Newton iteration for the Fermi level
+//                  (dft/KSDFTEnergyFunctional.cc:76-124) and occupations
+//                  (main.cc:1239-1272).
+//
+// FP64 throughout: these are the quantities the method keeps in double.
+
+#include <cmath>
+#include "ttg_internal.cuh"
+
+namespace ttg {
+namespace {
+
+constexpr int TM = 64, TN = 64, TK = 16;
+
+// S_partial[z] = X[rows_z]^T Y[rows_z]; 256 threads, 4x4 outputs each.
+__global__ void __launch_bounds__(256) k_gram_tn(const double* __restrict__ X,
+                                                 const double* __restrict__ Y, int64_t n,
+                                                 int k, int64_t ld, int64_t rows_per_split,
+                                                 double* __restrict__ part) {
+  __shared__ double sX[TK][TM + 1];
+  __shared__ double sY[TK][TN + 1];
+  const int p0 = blockIdx.x * TM, q0 = blockIdx.y * TN;
+  const int64_t r0 = (int64_t)blockIdx.z * rows_per_split;
+  const int64_t r1 = (n < r0 + rows_per_split ? n : r0 + rows_per_split);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  for (int64_t rb = r0; rb < r1; rb += TK) {
+    for (int i = threadIdx.x; i < TK * TM; i += 256) {
+      const int rr = i / TM, cc = i % TM;
+      const int64_t row = rb + rr;
+      sX[rr][cc] = (row < r1 && p0 + cc < k) ? X[row * ld + p0 + cc] : 0.0;
+      sY[rr][cc] = (row < r1 && q0 + cc < k) ? Y[row * ld + q0 + cc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < TK; ++t) {
+      double a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = sX[t][ty + 16 * u];
+        b[u] = sY[t][tx + 16 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  double* out = part + (int64_t)blockIdx.z * k * k;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int p = p0 + ty + 16 * u, q = q0 + tx + 16 * v;
+      if (p < k && q < k) out[p + (int64_t)q * k] = acc[u][v];   // column-major
+    }
+}
+
+__global__ void k_reduce_splits(const double* __restrict__ part, int nsplit, int64_t kk,
+                                double* __restrict__ S) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < kk;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int z = 0; z < nsplit; ++z) s += part[(int64_t)z * kk + i];
+    S[i] = s;
+  }
+}
+
+// out[i, q] = sum_p X[i, p] * Qop[p, q],  Qop = Q or Q^T (Q column-major k x k)
+__global__ void __launch_bounds__(256) k_gemm_nn(const double* __restrict__ X,
+                                                 const double* __restrict__ Q,
+                                                 double* __restrict__ out, int64_t n, int k,
+                                                 int64_t ld, int transQ) {
+  __shared__ double sX[TM][TK + 1];
+  __shared__ double sQ[TK][TN + 1];
+  const int64_t i0 = (int64_t)blockIdx.x * TM;
+  const int q0 = blockIdx.y * TN;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  for (int pb = 0; pb < k; pb += TK) {
+    for (int e = threadIdx.x; e < TM * TK; e += 256) {
+      const int rr = e / TK, cc = e % TK;
+      const int64_t row = i0 + rr;
+      sX[rr][cc] = (row < n && pb + cc < k) ? X[row * ld + pb + cc] : 0.0;
+    }
+    for (int e = threadIdx.x; e < TK * TN; e += 256) {
+      const int rr = e / TN, cc = e % TN;
+      const int p = pb + rr, q = q0 + cc;
+      double v = 0.0;
+      if (p < k && q < k) v = transQ ? Q[q + (int64_t)p * k] : Q[p + (int64_t)q * k];
+      sQ[rr][cc] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < TK; ++t) {
+      double a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = sX[ty + 16 * u][t];
+        b[u] = sQ[t][tx + 16 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int64_t i = i0 + ty + 16 * u;
+      const int q = q0 + tx + 16 * v;
+      if (i < n && q < k) out[i * ld + q] = acc[u][v];
+    }
+}
+
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  const int nw = (blockDim.x + 31) / 32;
+  for (int i = 0; i < nw; ++i) s += red[i];
+  return s;
+}
+
+// Right-looking Cholesky in place on the lower triangle of A (column-major),
+// then Linv = L^-1 (lower).  One CTA.  status[0] = 0 ok, j+1 if pivot j <= 0.
+__global__ void __launch_bounds__(1024) k_cholesky_inv(double* A, double* Linv, int k,
+                                                       int* status) {
+  __shared__ double s_piv;
+  __shared__ int s_bad;
+  // diagonal of S before the factorisation, for the relative pivot test
+  double* diag0 = Linv;
+  for (int j = threadIdx.x; j < k; j += blockDim.x) diag0[j] = A[j + (int64_t)j * k];
+  if (threadIdx.x == 0) s_bad = 0;
+  __syncthreads();
+  for (int j = 0; j < k; ++j) {
+    if (threadIdx.x == 0) {
+      const double d = A[j + (int64_t)j * k];
+      const double s0 = diag0[j];
+      // not positive definite in FP64: pivot lost 12+ digits of its diagonal
+      if (!(d > 1e-12 * s0) || !(s0 > 0.0) || !isfinite(d)) s_bad = j + 1;
+      s_piv = d > 0.0 ? sqrt(d) : 1.0;
+    }
+    __syncthreads();
+    if (s_bad) break;
+    const double piv = s_piv;
+    for (int i = j + threadIdx.x; i < k; i += blockDim.x) {
+      const double v = (i == j) ? piv : A[i + (int64_t)j * k] / piv;
+      A[i + (int64_t)j * k] = v;
+    }
+    __syncthreads();
+    // trailing update of the lower triangle: A[i,l] -= L[i,j] L[l,j], j<l<=i
+    const int m = k - j - 1;
+    for (int64_t e = threadIdx.x; e < (int64_t)m * m; e += blockDim.x) {
+      const int ii = (int)(e % m), ll = (int)(e / m);
+      if (ll > ii) continue;
+      const int i = j + 1 + ii, l = j + 1 + ll;
+      A[i + (int64_t)l * k] -= A[i + (int64_t)j * k] * A[l + (int64_t)j * k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) status[0] = s_bad;
+  if (s_bad) return;
+  // Linv: row by row, X[i][j] = (delta_ij - sum_{p=j}^{i-1} L[i,p] X[p][j]) / L[i,i]
+  __syncthreads();
+  for (int64_t e = threadIdx.x; e < (int64_t)k * k; e += blockDim.x) Linv[e] = 0.0;
+  __syncthreads();
+  for (int i = 0; i < k; ++i) {
+    const double lii = A[i + (int64_t)i * k];
+    for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+      double s = (i == j) ? 1.0 : 0.0;
+      for (int p = j; p < i; ++p) s -= A[i + (int64_t)p * k] * Linv[p + (int64_t)j * k];
+      Linv[i + (int64_t)j * k] = s / lii;
+    }
+    __syncthreads();
+  }
+}
+
+// Cyclic Jacobi on a symmetric k x k column-major A (overwritten), V = eigvecs.
+// One CTA.  status[0]: 0 converged, 1 not converged within max_sweeps.
+__global__ void __launch_bounds__(1024) k_jacobi(double* A, double* V, double* w, int k,
+                                                 int max_sweeps, double tol, int* status,
+                                                 double* cs_buf) {
+  __shared__ double red[32];
+  const int m = (k % 2 == 0) ? k : k + 1;      // players incl. a dummy
+  const int npairs = m / 2;
+  double* cs = cs_buf;                          // [npairs][2]
+  int* pq = reinterpret_cast<int*>(cs_buf + 2 * npairs);
+  for (int64_t e = threadIdx.x; e < (int64_t)k * k; e += blockDim.x) {
+    const int i = (int)(e % k), j = (int)(e / k);
+    V[e] = (i == j) ? 1.0 : 0.0;
+  }
+  // Frobenius norm for the stopping test
+  double loc = 0.0;
+  for (int64_t e = threadIdx.x; e < (int64_t)k * k; e += blockDim.x) loc += A[e] * A[e];
+  const double fro2 = block_sum(loc, red);
+  int converged = 0;
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    double off = 0.0;
+    for (int64_t e = threadIdx.x; e < (int64_t)k * k; e += blockDim.x) {
+      const int i = (int)(e % k), j = (int)(e / k);
+      if (i != j) off += A[e] * A[e];
+    }
+    off = block_sum(off, red);
+    // rounding leaves off-diagonal entries of order eps*|A|, so the threshold
+    // grows with k: (tol^2 * k) * |A|_F^2
+    if (off <= tol * tol * (double)k * fro2 || off == 0.0) {
+      converged = 1;
+      break;
+    }
+    for (int r = 0; r < m - 1; ++r) {
+      // pairs of this round: player 0 fixed, the others rotate
+      for (int i = threadIdx.x; i < npairs; i += blockDim.x) {
+        const int a = (i == 0) ? 0 : 1 + ((i - 1 + r) % (m - 1));
+        const int bj = m - 1 - i;
+        const int b = 1 + ((bj - 1 + r) % (m - 1));
+        int p = min(a, b), q = max(a, b);
+        double c = 1.0, s = 0.0;
+        if (q < k) {
+          const double apq = A[p + (int64_t)q * k];
+          if (apq != 0.0) {
+            const double app = A[p + (int64_t)p * k], aqq = A[q + (int64_t)q * k];
+            const double theta = (aqq - app) / (2.0 * apq);
+            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        } else {
+          q = -1;
+        }
+        cs[2 * i] = c;
+        cs[2 * i + 1] = s;
+        pq[2 * i] = p;
+        pq[2 * i + 1] = q;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (int64_t e = threadIdx.x; e < (int64_t)npairs * k; e += blockDim.x) {
+        const int i = (int)(e / k), j = (int)(e % k);
+        const int p = pq[2 * i], q = pq[2 * i + 1];
+        if (q < 0) continue;
+        const double c = cs[2 * i], s = cs[2 * i + 1];
+        if (s == 0.0) continue;
+        const double ap = A[p + (int64_t)j * k], aq = A[q + (int64_t)j * k];
+        A[p + (int64_t)j * k] = c * ap - s * aq;
+        A[q + (int64_t)j * k] = s * ap + c * aq;
+      }
+      __syncthreads();
+      // columns: A <- A J, V <- V J
+      for (int64_t e = threadIdx.x; e < (int64_t)npairs * k; e += blockDim.x) {
+        const int i = (int)(e / k), j = (int)(e % k);
+        const int p = pq[2 * i], q = pq[2 * i + 1];
+        if (q < 0) continue;
+        const double c = cs[2 * i], s = cs[2 * i + 1];
+        if (s == 0.0) continue;
+        const double ap = A[j + (int64_t)p * k], aq = A[j + (int64_t)q * k];
+        A[j + (int64_t)p * k] = c * ap - s * aq;
+        A[j + (int64_t)q * k] = s * ap + c * aq;
+        const double vp = V[j + (int64_t)p * k], vq = V[j + (int64_t)q * k];
+        V[j + (int64_t)p * k] = c * vp - s * vq;
+        V[j + (int64_t)q * k] = s * vp + c * vq;
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < k; i += blockDim.x) w[i] = A[i + (int64_t)i * k];
+  if (threadIdx.x == 0) status[0] = converged ? 0 : 1;
+}
+
+// Sort eigenpairs ascending (stable rank sort), normalise each eigenvector's
+// sign so that its largest-magnitude component is positive.
+__global__ void k_sort_eig(const double* w, const double* V, double* w_out, double* V_out,
+                           int k) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < k; j += gridDim.x * blockDim.x) {
+    int rank = 0;
+    const double wj = w[j];
+    for (int i = 0; i < k; ++i) rank += (w[i] < wj) || (w[i] == wj && i < j);
+    w_out[rank] = wj;
+    double big = 0.0;
+    int ib = 0;
+    for (int i = 0; i < k; ++i) {
+      const double a = fabs(V[i + (int64_t)j * k]);
+      if (a > big) { big = a; ib = i; }
+    }
+    const double sg = V[ib + (int64_t)j * k] < 0 ? -1.0 : 1.0;
+    for (int i = 0; i < k; ++i) V_out[i + (int64_t)rank * k] = sg * V[i + (int64_t)j * k];
+  }
+}
+
+__global__ void k_symmetrize(double* A, int k) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)k * k;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % k), j = (int)(e / k);
+    if (i < j) {
+      const double v = 0.5 * (A[i + (int64_t)j * k] + A[j + (int64_t)i * k]);
+      A[i + (int64_t)j * k] = v;
+      A[j + (int64_t)i * k] = v;
+    }
+  }
+}
+
+__global__ void k_cm_to_rows(const double* __restrict__ src, int64_t lds, double* __restrict__ dst,
+                             int64_t ldd, int64_t n, int k) {
+  // tile transpose 32x32
+  __shared__ double t[32][33];
+  const int64_t i0 = (int64_t)blockIdx.x * 32;
+  const int j0 = blockIdx.y * 32;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int j = j0 + y;
+    const int64_t i = i0 + threadIdx.x;
+    t[y][threadIdx.x] = (i < n && j < k) ? src[i + (int64_t)j * lds] : 0.0;
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int64_t i = i0 + y;
+    const int j = j0 + threadIdx.x;
+    if (i < n && j < k) dst[i * ldd + j] = t[threadIdx.x][y];
+  }
+}
+
+__global__ void k_rows_to_cm(const double* __restrict__ src, int64_t lds, double* __restrict__ dst,
+                             int64_t ldd, int64_t n, int k) {
+  __shared__ double t[32][33];
+  const int64_t i0 = (int64_t)blockIdx.x * 32;
+  const int j0 = blockIdx.y * 32;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int64_t i = i0 + y;
+    const int j = j0 + threadIdx.x;
+    t[y][threadIdx.x] = (i < n && j < k) ? src[i * lds + j] : 0.0;
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int j = j0 + y;
+    const int64_t i = i0 + threadIdx.x;
+    if (i < n && j < k) dst[i + (int64_t)j * ldd] = t[threadIdx.x][y];
+  }
+}
+
+// One Lanczos step on strided vectors (stride ld).  Single CTA.
+//   f = hv - beta_prev v0;  alpha = v.f;  f -= alpha v;  beta = |f|;
+//   v0 <- v;  v <- f / beta;  ab[2*it] = alpha, ab[2*it+1] = beta.
+__global__ void __launch_bounds__(1024) k_lanczos_step(double* v, double* v0, const double* hv,
+                                                       int64_t n, int64_t ld, double* ab,
+                                                       int it) {
+  __shared__ double red[32];
+  const double beta_prev = it > 0 ? ab[2 * (it - 1) + 1] : 0.0;
+  double d = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double f = hv[i * ld] - beta_prev * v0[i * ld];
+    d += v[i * ld] * f;
+  }
+  const double alpha = block_sum(d, red);
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double f = hv[i * ld] - beta_prev * v0[i * ld] - alpha * v[i * ld];
+    s += f * f;
+  }
+  const double beta = sqrt(block_sum(s, red));
+  const double inv = beta > 0 ? 1.0 / beta : 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double f = hv[i * ld] - beta_prev * v0[i * ld] - alpha * v[i * ld];
+    const double vi = v[i * ld];
+    v0[i * ld] = vi;
+    v[i * ld] = f * inv;
+  }
+  if (threadIdx.x == 0) {
+    ab[2 * it] = alpha;
+    ab[2 * it + 1] = beta;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_normalize(double* v, int64_t n, int64_t ld) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += v[i * ld] * v[i * ld];
+  const double nrm = sqrt(block_sum(s, red));
+  const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) v[i * ld] *= inv;
+}
+
+// Fermi level by Newton (dft/KSDFTEnergyFunctional.cc:76-124) and occupancy
+// factors (main.cc:1247-1260).  One CTA.  out[0] = mu, out[1] = iterations,
+// out[2] = final |sum - Ne|.
+__global__ void __launch_bounds__(256) k_fermi(const double* eig, int k, double ne, double kT,
+                                               int max_iter, double* occ, double* out) {
+  __shared__ double red[32];
+  int occ_num = (int)(ne / 2.0);
+  if (((long long)ne) % 2 == 1) occ_num += 1;
+  occ_num = max(1, min(occ_num, k));
+  double mu = eig[occ_num - 1];
+  int it = 0;
+  double func = 0.0;
+  for (; it < max_iter; ++it) {
+    double sf = 0.0, sd = 0.0;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+      const double arg = (eig[i] - mu) / kT;
+      if (arg <= 0.0) {
+        const double term = 1.0 / (1.0 + exp(arg));
+        sf += 2.0 * term;
+        sd += 2.0 * (exp(arg) / kT) * term * term;
+      } else {
+        const double term = 1.0 / (1.0 + exp(-arg));
+        sf += 2.0 * exp(-arg) * term;
+        sd += 2.0 * (exp(-arg) / kT) * term * term;
+      }
+    }
+    sf = block_sum(sf, red);
+    sd = block_sum(sd, red);
+    func = sf - ne;
+    mu = mu - func / sd;
+    if (fabs(func) <= 1.0e-8) break;
+  }
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    const double term = (eig[i] - mu) / kT;
+    occ[i] = term <= 0.0 ? 1.0 / (1.0 + exp(term)) : exp(-term) / (1.0 + exp(-term));
+  }
+  if (threadIdx.x == 0) {
+    out[0] = mu;
+    out[1] = (double)it;
+    out[2] = fabs(func);
+  }
+}
+
+}  // namespace
+
+ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* S) {
+  const int tp = (k + TM - 1) / TM, tq = (k + TN - 1) / TN;
+  const int tiles = tp * tq;
+  int64_t nsplit = (2 * 152 + tiles - 1) / tiles;
+  nsplit = std::min<int64_t>(nsplit, (op->n + 255) / 256);
+  if (nsplit < 1) nsplit = 1;
+  const int64_t need = nsplit * (int64_t)k * k * sizeof(double);
+  if ((int64_t)op->partial.bytes < need) TTG_TRY(op->partial.alloc(need));
+  const int64_t rows = (op->n + nsplit - 1) / nsplit;
+  k_gram_tn<<<dim3(tp, tq, (unsigned)nsplit), 256, 0, op->stream>>>(X, Y, op->n, k, op->ld, rows,
+                                                                   op->partial.as<double>());
+  TTG_LAUNCHED(op);
+  const int64_t kk = (int64_t)k * k;
+  k_reduce_splits<<<(unsigned)std::min<int64_t>((kk + 255) / 256, 1024), 256, 0, op->stream>>>(
+      op->partial.as<double>(), (int)nsplit, kk, S);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status gemm_nn_small(ttg_op* op, const double* X, const double* Q, double* out, int k,
+                         int transQ) {
+  dim3 grid((unsigned)((op->n + TM - 1) / TM), (unsigned)((k + TN - 1) / TN));
+  k_gemm_nn<<<grid, 256, 0, op->stream>>>(X, Q, out, op->n, k, op->ld, transQ);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_status) {
+  k_cholesky_inv<<<1, 1024, 0, op->stream>>>(S, Linv, k, d_status);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status syev_jacobi(ttg_op* op, double* A, double* V, double* w, int k, int* d_status) {
+  // scratch layout in op->scal (doubles): [kScalJacobi, +4(k+2)) rotations and
+  // pair ids, then k unsorted eigenvalues.  Unsorted eigenvectors go to kk2.
+  const int64_t need = (kScalJacobi + 4 * (int64_t)(k + 2) + k) * (int64_t)sizeof(double);
+  if ((int64_t)op->scal.bytes < need || (int64_t)op->kk2.bytes < (int64_t)k * k * 8)
+    return TTG_BAD_ARG;
+  double* cs = op->scal.as<double>() + kScalJacobi;
+  double* wtmp = cs + 4 * (k + 2);
+  k_symmetrize<<<64, 256, 0, op->stream>>>(A, k);
+  TTG_LAUNCHED(op);
+  k_jacobi<<<1, 1024, 0, op->stream>>>(A, op->kk2.as<double>(), wtmp, k, 60, 1e-14, d_status,
+                                       cs);
+  TTG_LAUNCHED(op);
+  k_sort_eig<<<(k + 127) / 128, 128, 0, op->stream>>>(wtmp, op->kk2.as<double>(), w, V, k);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status colmajor_to_rows(ttg_op* op, const double* src, int64_t ld_src, double* dst,
+                            int64_t ld_dst, int64_t n, int k) {
+  dim3 grid((unsigned)((n + 31) / 32), (unsigned)((k + 31) / 32));
+  k_cm_to_rows<<<grid, dim3(32, 8), 0, op->stream>>>(src, ld_src, dst, ld_dst, n, k);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status rows_to_colmajor(ttg_op* op, const double* src, int64_t ld_src, double* dst,
+                            int64_t ld_dst, int64_t n, int k) {
+  dim3 grid((unsigned)((n + 31) / 32), (unsigned)((k + 31) / 32));
+  k_rows_to_cm<<<grid, dim3(32, 8), 0, op->stream>>>(src, ld_src, dst, ld_dst, n, k);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status lanczos_step(ttg_op* op, double* v, double* v0, const double* hv, double* ab, int it) {
+  k_lanczos_step<<<1, 1024, 0, op->stream>>>(v, v0, hv, op->n, op->ld, ab, it);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status normalize(ttg_op* op, double* v) {
+  k_normalize<<<1, 1024, 0, op->stream>>>(v, op->n, op->ld);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status fermi(ttg_op* op, const double* eig, int k, double ne, double kT, int max_iter,
+                 double* occ, double* out) {
+  k_fermi<<<1, 256, 0, op->stream>>>(eig, k, ne, kT, max_iter, occ, out);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+}  // namespace ttg

@@ -1,0 +1,211 @@
+// Host operator producer: assembles the projected Kohn-Sham Hamiltonian H_loc
+// in a separable (Tucker) basis as a truncated CSR matrix, and the nonlocal
+// projector matrix C_nloc.
+//
+// Follows ProjectHamiltonianSparse::Create_Hloc
+// (dft/ProjectHamiltonianSparse.cc:330-575): for row I = (xI, yI, zI) with
+// I = xI + rx*(yI + ry*zI) (x fastest, :420-433) the entries are
+//   0.5*(DX[xI,xJ] MY[yI,yJ] MZ[zI,zJ] + MX DY MZ + MX MY DZ)      (:480-491)
+//   + sum_abc G_abc PX_a[xI,xJ] PY_b[yI,yJ] PZ_c[zI,zJ]             (:516-543)
+// and only |h| > truncation is kept (:545-548).  The potential here is given
+// in canonical (CP) form, sum_t c_t PX_t (x) PY_t (x) PZ_t, which is a Tucker
+// form with a superdiagonal core; a dense Tucker core is expanded by the
+// caller into this form.
+//
+// The assembly is row-parallel (OpenMP) and prunes terms whose 1-D factors
+// cannot reach the truncation threshold, so that large operators assemble in
+// seconds.  Host-only code: no CUDA, no torch.
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct Sparse1D {
+  // row-wise sparse copy of an r x r matrix (entries above a drop tolerance)
+  std::vector<int64_t> ptr;
+  std::vector<int> col;
+  std::vector<double> val;
+  std::vector<double> rowmax;
+};
+
+Sparse1D make_sparse(const double* m, int r, double drop) {
+  Sparse1D s;
+  s.ptr.assign(r + 1, 0);
+  s.rowmax.assign(r, 0.0);
+  double amax = 0.0;
+  for (int i = 0; i < r * r; ++i) amax = std::max(amax, std::fabs(m[i]));
+  double thr = drop * amax;
+  for (int i = 0; i < r; ++i) {
+    for (int j = 0; j < r; ++j) {
+      double v = m[(int64_t)i * r + j];
+      if (std::fabs(v) > thr) {
+        s.col.push_back(j);
+        s.val.push_back(v);
+        s.rowmax[i] = std::max(s.rowmax[i], std::fabs(v));
+      }
+    }
+    s.ptr[i + 1] = (int64_t)s.col.size();
+  }
+  return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Assemble H_loc.
+//   r[3]            : Tucker basis ranks (rx, ry, rz)
+//   MX,MY,MZ        : 1-D overlap matrices, row-major r x r
+//   DX,DY,DZ        : 1-D stiffness matrices (int psi' psi'), row-major r x r
+//   nterm, coef     : CP potential, coef[t]
+//   PX,PY,PZ        : nterm x r x r potential overlap matrices (row-major)
+//   truncation      : keep |h| > truncation
+//   drop            : relative drop tolerance for pruning 1-D factors (1e-15 typ.)
+// Two-phase API: call with vals == nullptr to get row_ptr (size N+1) filled,
+// then call again with col/vals of size row_ptr[N].
+// Returns 0 on success, negative on bad arguments.
+int ttg_host_assemble_hloc(const int* r, const double* MX, const double* MY,
+                           const double* MZ, const double* DX, const double* DY,
+                           const double* DZ, int nterm, const double* coef,
+                           const double* PX, const double* PY, const double* PZ,
+                           double truncation, double drop, int64_t* row_ptr,
+                           int* col, double* vals) {
+  if (!r || r[0] <= 0 || r[1] <= 0 || r[2] <= 0 || nterm < 0 || !row_ptr) return -1;
+  const int rx = r[0], ry = r[1], rz = r[2];
+  const int64_t N = (int64_t)rx * ry * rz;
+  Sparse1D sMX = make_sparse(MX, rx, drop), sMY = make_sparse(MY, ry, drop),
+           sMZ = make_sparse(MZ, rz, drop);
+  Sparse1D sDX = make_sparse(DX, rx, drop), sDY = make_sparse(DY, ry, drop),
+           sDZ = make_sparse(DZ, rz, drop);
+  std::vector<Sparse1D> sPX(nterm), sPY(nterm), sPZ(nterm);
+  for (int t = 0; t < nterm; ++t) {
+    sPX[t] = make_sparse(PX + (int64_t)t * rx * rx, rx, drop);
+    sPY[t] = make_sparse(PY + (int64_t)t * ry * ry, ry, drop);
+    sPZ[t] = make_sparse(PZ + (int64_t)t * rz * rz, rz, drop);
+  }
+  const bool fill = (vals != nullptr);
+  const double prune = truncation * 1e-6;
+
+#pragma omp parallel
+  {
+    std::vector<double> row(N, 0.0);
+    std::vector<char> touched(N, 0);
+    std::vector<int> touched_list;
+    touched_list.reserve(1 << 16);
+    auto add = [&](int64_t J, double v) {
+      if (!touched[J]) {
+        touched[J] = 1;
+        touched_list.push_back((int)J);
+      }
+      row[J] += v;
+    };
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t I = 0; I < N; ++I) {
+      const int xI = (int)(I % rx);
+      const int yI = (int)((I / rx) % ry);
+      const int zI = (int)(I / ((int64_t)rx * ry));
+      // kinetic: 0.5*(DX MY MZ + MX DY MZ + MX MY DZ)
+      const Sparse1D* A[3][3] = {{&sDX, &sMY, &sMZ}, {&sMX, &sDY, &sMZ}, {&sMX, &sMY, &sDZ}};
+      for (int term = 0; term < 3; ++term) {
+        const Sparse1D &ax = *A[term][0], &ay = *A[term][1], &az = *A[term][2];
+        for (int64_t pz = az.ptr[zI]; pz < az.ptr[zI + 1]; ++pz) {
+          const int zJ = az.col[pz];
+          const double vz = 0.5 * az.val[pz];
+          for (int64_t py = ay.ptr[yI]; py < ay.ptr[yI + 1]; ++py) {
+            const int yJ = ay.col[py];
+            const double vyz = vz * ay.val[py];
+            const int64_t base = (int64_t)rx * (yJ + (int64_t)ry * zJ);
+            for (int64_t px = ax.ptr[xI]; px < ax.ptr[xI + 1]; ++px)
+              add(base + ax.col[px], vyz * ax.val[px]);
+          }
+        }
+      }
+      // potential: sum_t coef_t PX_t PY_t PZ_t
+      for (int t = 0; t < nterm; ++t) {
+        const Sparse1D &px = sPX[t], &py = sPY[t], &pz = sPZ[t];
+        const double bound = std::fabs(coef[t]) * px.rowmax[xI] * py.rowmax[yI] * pz.rowmax[zI];
+        if (bound <= prune) continue;
+        for (int64_t qz = pz.ptr[zI]; qz < pz.ptr[zI + 1]; ++qz) {
+          const int zJ = pz.col[qz];
+          const double wz = coef[t] * pz.val[qz];
+          if (std::fabs(wz) * py.rowmax[yI] * px.rowmax[xI] <= prune) continue;
+          for (int64_t qy = py.ptr[yI]; qy < py.ptr[yI + 1]; ++qy) {
+            const int yJ = py.col[qy];
+            const double w = wz * py.val[qy];
+            if (std::fabs(w) * px.rowmax[xI] <= prune) continue;
+            const int64_t base = (int64_t)rx * (yJ + (int64_t)ry * zJ);
+            for (int64_t qx = px.ptr[xI]; qx < px.ptr[xI + 1]; ++qx)
+              add(base + px.col[qx], w * px.val[qx]);
+          }
+        }
+      }
+      std::sort(touched_list.begin(), touched_list.end());
+      int64_t cnt = 0;
+      int64_t out = fill ? row_ptr[I] : 0;
+      for (int J : touched_list) {
+        const double v = row[J];
+        if (std::fabs(v) > truncation) {
+          if (fill) {
+            col[out] = J;
+            vals[out] = v;
+            ++out;
+          }
+          ++cnt;
+        }
+        row[J] = 0.0;
+        touched[J] = 0;
+      }
+      touched_list.clear();
+      if (!fill) row_ptr[I + 1] = cnt;
+    }
+  }
+  if (!fill) {
+    row_ptr[0] = 0;
+    for (int64_t I = 0; I < N; ++I) row_ptr[I + 1] += row_ptr[I];
+  }
+  return 0;
+}
+
+// Separable nonlocal projector matrix C (nproj x N, CSR):
+//   C[a, J] = cx[a, xJ] * cy[a, yJ] * cz[a, zJ], kept where |C| > tol.
+// Follows ProjectHamiltonianSparse::Create_Cnloc
+// (dft/ProjectHamiltonianSparse.cc:83-328) for projectors whose Tucker form is
+// rank one.  Two-phase like ttg_host_assemble_hloc.
+int ttg_host_assemble_cnloc(const int* r, int nproj, const double* cx,
+                            const double* cy, const double* cz, double tol,
+                            int64_t* row_ptr, int* col, double* vals) {
+  if (!r || nproj < 0 || !row_ptr) return -1;
+  const int rx = r[0], ry = r[1], rz = r[2];
+  const bool fill = (vals != nullptr);
+  row_ptr[0] = 0;
+  for (int a = 0; a < nproj; ++a) {
+    int64_t out = fill ? row_ptr[a] : 0;
+    int64_t cnt = 0;
+    for (int zJ = 0; zJ < rz; ++zJ)
+      for (int yJ = 0; yJ < ry; ++yJ) {
+        const double wyz = cy[(int64_t)a * ry + yJ] * cz[(int64_t)a * rz + zJ];
+        for (int xJ = 0; xJ < rx; ++xJ) {
+          const double v = wyz * cx[(int64_t)a * rx + xJ];
+          if (std::fabs(v) > tol) {
+            if (fill) {
+              col[out] = xJ + rx * (yJ + ry * zJ);
+              vals[out] = v;
+              ++out;
+            }
+            ++cnt;
+          }
+        }
+      }
+    if (!fill) row_ptr[a + 1] = row_ptr[a] + cnt;
+  }
+  return 0;
+}
+
+}  // extern "C"
