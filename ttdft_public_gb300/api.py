@@ -19,6 +19,7 @@ library status instead of terminating the process.
 from __future__ import annotations
 
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -86,6 +87,7 @@ class Operator:
         self.n = h.n_rows
         self.max_k = max_k
         self._keep = None
+        self._blocks = weakref.WeakSet()
 
     def info(self) -> dict:
         inf = _lib.TtgOpInfo()
@@ -108,6 +110,8 @@ class Operator:
 
     def close(self):
         if getattr(self, "h", None):
+            for b in list(self._blocks):
+                b.close()
             _lib.ttg().ttg_op_destroy(self.h)
             self.h = None
 
@@ -127,6 +131,7 @@ class Mat:
         handle = ctypes.c_void_p()
         check(_lib.ttg().ttg_block_create(op.h, k, ctypes.byref(handle)), "ttg_block_create")
         self.h = handle
+        op._blocks.add(self)
         if data is not None:
             self.set(data)
 

@@ -193,7 +193,8 @@ ttg_status ttg_block_create(ttg_op* op, int32_t k, ttg_block** out) {
 
 ttg_status ttg_block_destroy(ttg_block* b) {
   if (!b) return TTG_BAD_ARG;
-  if (b->op) cudaStreamSynchronize(b->op->stream);
+  // cudaFree waits for the device; the op may already be gone, so it is not
+  // touched here.
   b->x.release();
   delete b;
   return TTG_OK;
