@@ -136,6 +136,19 @@ ttg_status ttg_apply_h(ttg_op* op, const ttg_block* X, ttg_block* HX);
  * NULL when only the device copy is wanted (kept inside the op). */
 ttg_status ttg_gram(ttg_op* op, const ttg_block* X, const ttg_block* Y, double* s_host);
 
+/* S = X^T Y like ttg_gram, for callers that cannot allocate device memory
+ * (memory-pool or arena owners, plugins whose host forbids cudaMalloc after
+ * start-up, code that must not synchronise the device).  No counterpart in
+ * the reference.  X and Y are device pointers, row-major n x k with leading
+ * dimension ld; S is a device pointer, k x k column-major; stream may be NULL.
+ * Allocates nothing: the split-row partial sums live in a fixed 16 MiB
+ * __device__ array that every GPU loading this library holds until exit, so
+ * k*k must not exceed 2,097,152 (k <= 1448), else TTG_BAD_ARG.  The first call
+ * on a device looks up that array's address and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+ttg_status ttg_gram_noalloc(const double* x_dev, const double* y_dev, int64_t n, int32_t k,
+                            int64_t ld, double* s_dev, void* stream);
+
 /* Cholesky-QR in FP64: S = X^T X = L L^T, X <- X L^-T.  Replaces MultTM::orth
  * (eigensolver/MultTm.h:39, eigensolver/MultTm.cu:226-467).  Returns
  * TTG_NOT_SPD (X untouched) when S is not numerically positive definite. */

@@ -70,6 +70,7 @@ _SIGS = {
     "ttg_cheb_filter": [c_vp, c_vp, c_i32, c_dbl, c_dbl, c_dbl, TtgSched],
     "ttg_apply_h": [c_vp, c_vp, c_vp],
     "ttg_gram": [c_vp, c_vp, c_vp, c_vp],
+    "ttg_gram_noalloc": [c_vp, c_vp, c_i64, c_i32, c_i64, c_vp, c_vp],
     "ttg_chol_qr": [c_vp, c_vp],
     "ttg_syev": [c_vp, c_i32, c_vp, c_vp, c_vp],
     "ttg_rayleigh_ritz": [c_vp, c_vp, c_i32, c_vp, c_vp],

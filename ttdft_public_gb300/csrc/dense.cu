@@ -21,7 +21,9 @@
 //
 // FP64 throughout: these are the quantities the method keeps in double.
 
+#include <algorithm>
 #include <cmath>
+#include <mutex>
 #include "ttg_internal.cuh"
 
 namespace ttg {
@@ -535,3 +537,84 @@ ttg_status fermi(ttg_op* op, const double* eig, int k, double ne, double kT, int
 }
 
 }  // namespace ttg
+
+// ------------------------------------------------------------------------
+// Allocation-free Gram matrix.
+//
+// Some callers cannot call cudaMalloc: code running inside a memory pool or
+// an arena that owns all device memory, plugins whose host forbids driver
+// allocations after start-up, or callers that must not synchronise the
+// device (cudaMalloc/cudaFree can).  ttg_gram_noalloc computes the same
+// S = X^T Y as ttg_gram with caller-owned inputs and outputs, and keeps its
+// split-K partial sums in the fixed array below instead of allocating.
+//
+// The array is a file-scope __device__ variable: every GPU that loads this
+// library holds kNoAllocScratchDoubles doubles (16 MiB) until the process
+// exits.  All calls share it and it keeps the last call's contents; each call
+// overwrites every partial it later reads, so nothing needs clearing.  Calls
+// whose work overlaps on the GPU (different streams, or host threads) race on
+// it and must be serialised by the caller.
+// The host cannot use the array's name as a device address, so the first call
+// on each device looks the address up with cudaGetSymbolAddress (with that
+// device current) and caches it; that first call should come before any
+// stream capture.
+namespace {
+
+constexpr int64_t kNoAllocScratchDoubles = 2 * 1024 * 1024;
+__device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+constexpr int kMaxDevices = 64;
+double* g_noalloc_ptr[kMaxDevices] = {};
+std::mutex g_noalloc_mu;
+
+ttg_status noalloc_scratch(double** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return TTG_NO_DEVICE;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      fprintf(stderr, "ttg: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+      cudaGetLastError();
+      return TTG_CUDA_ERR;
+    }
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return TTG_OK;
+}
+
+}  // namespace
+
+extern "C" ttg_status ttg_gram_noalloc(const double* x_dev, const double* y_dev, int64_t n,
+                                       int32_t k, int64_t ld, double* s_dev, void* stream) {
+  if (!x_dev || !y_dev || !s_dev || n <= 0 || k <= 0 || ld < k) return TTG_BAD_ARG;
+  const int64_t kk = (int64_t)k * k;
+  if (kk > kNoAllocScratchDoubles) {
+    fprintf(stderr, "ttg_gram_noalloc: k = %d needs %lld scratch doubles, the maximum is %lld\n",
+            k, (long long)kk, (long long)kNoAllocScratchDoubles);
+    return TTG_BAD_ARG;
+  }
+  double* scratch = nullptr;
+  TTG_TRY(noalloc_scratch(&scratch));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int tp = (k + ttg::TM - 1) / ttg::TM, tq = (k + ttg::TN - 1) / ttg::TN;
+  const int tiles = tp * tq;
+  int64_t nsplit = (2 * 152 + tiles - 1) / tiles;
+  nsplit = std::min<int64_t>(nsplit, (n + 255) / 256);
+  nsplit = std::min<int64_t>(nsplit, kNoAllocScratchDoubles / kk);
+  if (nsplit < 1) nsplit = 1;
+  const int64_t rows = (n + nsplit - 1) / nsplit;
+  ttg::k_gram_tn<<<dim3(tp, tq, (unsigned)nsplit), 256, 0, st>>>(x_dev, y_dev, n, k, ld, rows,
+                                                                scratch);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return TTG_CUDA_ERR;
+  ttg::k_reduce_splits<<<(unsigned)std::min<int64_t>((kk + 255) / 256, 1024), 256, 0, st>>>(
+      scratch, (int)nsplit, kk, s_dev);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? TTG_OK : TTG_CUDA_ERR;
+}
