@@ -186,6 +186,27 @@ def run_ours(args, rank, world):
     dev_s = max_over_ranks(dev_ms / 1e3, world)
     sec_per_step = dev_s / args.steps
 
+    # ---- per-phase breakdown of one step (untimed for the headline)
+    phases = {}
+    ax = _ax(op, k)
+    t0 = time.perf_counter()
+    op.record(4)
+    api.ChebyShevFilter(sch).computeFilteredSubspace(None, ax, X, s.N, m, state["a"], upper,
+                                                     state["a0"])
+    op.record(5)
+    api.MultTM().orth(X)
+    op.record(6)
+    w_ph = api.rayleigh_ritz(op, X, rotate=True)
+    op.record(7)
+    mu, occ = api.fermi(op, w_ph, ne, kT)
+    op.record(8)
+    api.density(op, X, occ, s.basis)
+    op.record(9)
+    op.sync()
+    for name, (s0, s1) in {"filter": (4, 5), "cholesky_qr": (5, 6), "rayleigh_ritz": (6, 7),
+                           "fermi": (7, 8), "density": (8, 9)}.items():
+        phases[name] = round(op.elapsed_ms(s0, s1), 3)
+
     # ---- dominant kernel: one filter degree (fused SpMM + recurrence), FP32
     nnz = info["nnz_h"] + 2 * info["nnz_c"]
     n = s.N
@@ -236,7 +257,7 @@ def run_ours(args, rank, world):
                        "fill": info["fill"], "l2": "per-step working set > 129 MB L2 "
                        "(H values alone %.2f GB)" % (info["device_bytes"] / 1e9),
                        "parallelism": f"replicas x{world}", "system_gen_s": round(gen_s, 1)},
-            "roofline": {"bound": "hbm", "kernel": "k_cheb_step (FP32, one filter degree)",
+            "roofline": {"bound": "hbm", "kernel": "k_cheb_tc<float> (3xTF32 tensor-core SpMM + recurrence, one FP32 filter degree)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                          "bytes_per_launch": bytes_deg, "launch_ms": per_deg_s * 1e3,
@@ -244,6 +265,8 @@ def run_ours(args, rank, world):
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": n * k * 8,
                     "d2h_bytes_per_step": n * k * 8 + k * 8 + s.basis[0].nodal.shape[0] ** 3 * 8},
             "gpu_launches": launches,
+            "phases_ms": phases,
+            "tile_fill": info["tile_fill"],
             "clocks": ck,
             "cpu_baseline": cpu,
             "wall_s_timed": wall,

@@ -16,6 +16,7 @@ class ProjectHamiltonianSparse {
   Mat C_nloc_trans = nullptr; // N x nproj, AIJ (= C^T)
   std::vector<double> D;      // projector couplings
   Mat C = nullptr;            // nproj x N, AIJ, unscaled
+  int tucker_ranks[3] = {0, 0, 0};  // (rx, ry, rz) when known: enables 3-D row tiling
 
   // Takes H_loc, C (nproj x N) and D; builds C_nloc and C_nloc_trans.
   void set(Mat h_loc, Mat c, const std::vector<double>& d);

@@ -40,7 +40,8 @@ typedef enum {
 typedef enum {
   TTG_PREC_FP64 = 0,   /* H and the block in FP64, FP64 accumulation */
   TTG_PREC_FP32 = 1,   /* H and the block in FP32, FP32 accumulation */
-  TTG_PREC_BF16 = 2    /* H and the block stored in BF16, FP32 accumulation */
+  TTG_PREC_BF16 = 2,   /* H and the block stored in BF16, FP32 accumulation */
+  TTG_PREC_DF64 = 3    /* FP64 values as pairs of FP32 (~44 bits) on the FP32 pipes */
 } ttg_prec;
 
 /* Precision schedule of one Chebyshev filter call: the first `n_low` degrees
@@ -69,6 +70,9 @@ typedef struct {
   double fill;            /* (nnz_h + nnz_c^T) / (group_rows * stored_cols) */
   int64_t device_bytes;   /* HBM held by the operator */
   int64_t launches;       /* kernels this op has launched so far */
+  int64_t n_tiles;        /* 64-row tiles of the tensor-core format (0: none) */
+  int64_t tile_slots;     /* merged column slots over all tiles */
+  double tile_fill;       /* (nnz_h + nnz_c^T) / (64 * tile_slots) */
 } ttg_op_info_t;
 
 /* ---- device and operator ------------------------------------------------ */
@@ -91,6 +95,19 @@ ttg_status ttg_op_create(int64_t n, const int64_t* h_row_ptr, const int32_t* h_c
                          const double* h_val, int32_t nproj, const int64_t* c_row_ptr,
                          const int32_t* c_col, const double* c_val, const double* d,
                          int32_t max_k, ttg_op** out);
+/* As ttg_op_create, for an H_loc in a separable basis of Tucker ranks
+ * (rx, ry, rz), rows ordered I = x + rx*(y + ry*z) as Create_Hloc orders
+ * them (dft/ProjectHamiltonianSparse.cc:420-433).  The ranks let the library
+ * tile rows in 4 x 4 x 4 blocks for the tensor-core SpMM; NULL gives tiles of
+ * consecutive rows. */
+ttg_status ttg_op_create_tucker(int64_t n, const int64_t* h_row_ptr, const int32_t* h_col,
+                                const double* h_val, int32_t nproj, const int64_t* c_row_ptr,
+                                const int32_t* c_col, const double* c_val, const double* d,
+                                const int32_t* tucker_ranks, int32_t max_k, ttg_op** out);
+/* Arithmetic of the H X product inside ttg_rayleigh_ritz / ttg_chfsi_pass:
+ * TTG_PREC_DF64 (default: FP64-level accuracy at the FP32 rate) or
+ * TTG_PREC_FP64 (native FP64, the reference's arithmetic). */
+ttg_status ttg_op_set_rr_precision(ttg_op* op, int32_t prec);
 /* Replaces AX::free_mata_on_device / AX::~AX (eigensolver/MultCuda.cu:673-717). */
 ttg_status ttg_op_destroy(ttg_op* op);
 ttg_status ttg_op_info(const ttg_op* op, ttg_op_info_t* info);
@@ -184,6 +201,68 @@ ttg_status ttg_lanczos_bounds(ttg_op* op, const double* v0_host, int32_t max_ite
 ttg_status ttg_chfsi_pass(ttg_op* op, ttg_block* X, int32_t m, double a, double b,
                           double a0, ttg_sched sched, int32_t rotate, double* w_host);
 
+/* ---- operator values for a new potential (SCF) ----------------------------- */
+
+/* 1-D stiffness (int psi' psi') and overlap matrices of the basis, r_d x r_d
+ * row-major (dft/ProjectHamiltonianSparse.cc:577-676).  Needs an op created
+ * with ttg_op_create_tucker. */
+ttg_status ttg_op_set_kinetic(ttg_op* op, const double* dx, const double* dy, const double* dz,
+                              const double* mx, const double* my, const double* mz);
+/* Recompute the values of H_loc on its fixed pattern for an effective potential
+ * in Tucker form, V = sum_abc G_abc u_a v_b w_c (G x-fastest, ranks pot_ranks):
+ * H = 0.5 (DX MY MZ + MX DY MZ + MX MY DZ) + sum_abc G_abc PX_a (x) PY_b (x) PZ_c
+ * with PX_a[i][j] = int psi_i u_a psi_j given as (ra x rx x rx) row-major
+ * (Create_Hloc, dft/ProjectHamiltonianSparse.cc:330-575, on the device).
+ * Entries the pattern does not hold are not created. */
+ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const double* G,
+                                   const double* px, const double* py, const double* pz);
+
+/* ---- SCF grid kernels (FP64, device pointers, x-fastest fields) ------------ */
+
+/* Sequentially truncated HOSVD (TuckerMPI::STHOSVD as used at main.cc:951-955
+ * and tensor/TensorUtils.cc:245-264): per mode, the eigenvectors of the mode
+ * Gram matrix, keeping the smallest rank whose discarded eigenvalues sum to
+ * at most eps^2 ||T||^2 / 3 (capped by max_ranks when not NULL).  Outputs:
+ * ranks, core (x-fastest), factors u_d (n_d x r_d column-major) -- all device
+ * buffers sized for the caps. */
+ttg_status ttg_tucker_sthosvd(ttg_op* op, const double* t_dev, const int32_t* dims, double eps,
+                              const int32_t* max_ranks, int32_t* ranks_out, double* core_dev,
+                              double* u0_dev, double* u1_dev, double* u2_dev);
+/* core x1 U0 x2 U1 x3 U2 onto an n0 x n1 x n2 grid (Tucker::ttm chain). */
+ttg_status ttg_tucker_reconstruct(const double* core_dev, const int32_t* ranks,
+                                  const double* u0_dev, const double* u1_dev,
+                                  const double* u2_dev, const int32_t* dims, double* out_dev,
+                                  void* stream);
+/* LDA exchange-correlation potential (added to v when accumulate_v) and energy
+ * density e = eps_xc(rho) rho (dft/KSDFTPotential.cc:127-267,
+ * dft/KSDFTEnergyFunctional.cc:27-56).  v or e may be NULL. */
+ttg_status ttg_grid_lda(const double* rho_dev, int64_t n, double* v_dev, double* e_dev,
+                        int32_t accumulate_v, void* stream);
+/* result = sum f g wx wy wz (g may be NULL): compute3DIntegral
+ * (dft/KSDFTEnergyFunctional.cc:169-192) and the weighted inner products of
+ * the Anderson mixing (dft/AndersonMixing.cc:150-265).  Fixed summation order. */
+ttg_status ttg_grid_integrate(const double* f_dev, const double* g_dev, const int32_t* dims,
+                              const double* wx_dev, const double* wy_dev, const double* wz_dev,
+                              double* result, void* stream);
+/* out[i,j,l] (+)= sum_a coef[a] fx[a,i] fy[a,j] fz[a,l]: superposition of
+ * separable per-atom fields on a tensor grid -- the atomic-density initial
+ * guess (InitialGuess::initializeRhoFromRadiusFile, dft/InitialGuess.cc:
+ * 573-681) and the Gaussian-well local potential.  fx is (nterms x n0). */
+ttg_status ttg_grid_cp_sum(int32_t nterms, const double* coef_dev, const double* fx_dev,
+                           const double* fy_dev, const double* fz_dev, const int32_t* dims,
+                           double* out_dev, int32_t accumulate, void* stream);
+/* out -= sum_a z_a erf(|r - R_a| / width) / |r - R_a|: the exact electrostatic
+ * potential of Gaussian ionic charges (pos: natoms x 3), which makes the
+ * synthetic systems neutral under the Hartree term. */
+ttg_status ttg_grid_ion_potential(int32_t natoms, const double* pos_dev, const double* z_dev,
+                                  double width, const double* gx_dev, const double* gy_dev,
+                                  const double* gz_dev, const int32_t* dims, double* out_dev,
+                                  void* stream);
+/* out = sum_m coef[m] fields[m] (|.| when take_abs), up to 12 fields
+ * (dft/AndersonMixing.cc:267-316). */
+ttg_status ttg_grid_lincomb(int32_t nterms, const double* const* fields_dev, const double* coef,
+                            int64_t n, double* out_dev, int32_t take_abs, void* stream);
+
 /* ---- Fermi level, density, Hartree --------------------------------------- */
 
 /* Fermi level by Newton on sum_i 2 f_i = n_electrons and the occupations f_i.
@@ -226,6 +305,22 @@ ttg_status ttg_hartree(int32_t K, const double* alpha, const double* omega,
                        int32_t nx, int32_t ny, int32_t nz,
                        const double* x, const double* y, const double* z,
                        double* v_host, float* kernel_ms);
+
+/* Hartree energy of a Tucker density on its own quadrature grid,
+ *   E_H = 1/2 sum_q sum_q' w_q rho_q K(q, q') w_q' rho_q'
+ *       = 1/2 sum_t omega_t <G, G x1 Kx_t x2 Ky_t x3 Kz_t>,
+ *   Kx_t = (Wx Ux)^T E_t (Wx Ux),  E_t[q, q'] = exp(-alpha_t (xq_q - xq_q')^2),
+ * the quadrature of the term 1/2 int rho V_H(rho) of the total energy
+ * (main.cc:1315-1401 with V_H from dft/KSDFTPotential.cc:269-340), in FP64
+ * and exact to rounding without forming V_H on the grid.  ranks = (rx, ry,
+ * rz), G x fastest, nq[d] quadrature points xq_d with weights wq_d, U_d
+ * nq[d] x r[d] column-major; all host memory.  Needs no op. */
+ttg_status ttg_hartree_energy(int32_t K, const double* alpha, const double* omega,
+                              const int32_t* ranks, const double* G, const int32_t* nq,
+                              const double* xq, const double* yq, const double* zq,
+                              const double* wqx, const double* wqy, const double* wqz,
+                              const double* ux, const double* uy, const double* uz,
+                              double* energy);
 
 #ifdef __cplusplus
 }

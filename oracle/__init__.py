@@ -208,6 +208,24 @@ def hartree(alpha, omega, G, quad, Uq, grids):
     return V
 
 
+def hartree_energy(alpha, omega, G, quad, Uq):
+    """1/2 sum_qq' w rho K w rho of a Tucker density on its quadrature grid as
+    1/2 sum_t omega_t <G, G x1 Kx_t x2 Ky_t x3 Kz_t>, Kd_t = (W U)^T E_t (W U)
+    (the Hartree term of main.cc:1315-1401).  G as (rz, ry, rx)."""
+    alpha = np.asarray(alpha, np.float64)
+    Kd = []
+    for d in range(3):
+        x, w = quad[d]
+        E = np.exp(-alpha[:, None, None] * (x[None, :, None] - x[None, None, :]) ** 2)
+        WU = w[:, None] * Uq[d]
+        Kd.append(np.einsum("qa,tqp,pb->tab", WU, E, WU, optimize=True))
+    e = 0.0
+    for t in range(alpha.size):
+        T = np.einsum("cba,ia,jb,lc->lji", G, Kd[0][t], Kd[1][t], Kd[2][t], optimize=True)
+        e += omega[t] * float(np.sum(G * T))
+    return 0.5 * e
+
+
 def sad_density(atoms, grids, z_val=3.0, width=1.0):
     """Superposition of atomic densities (InitialGuess.cc:573-681): each atom a
     normalised Gaussian of z_val electrons (the synthetic atoms' radial

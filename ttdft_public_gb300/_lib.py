@@ -44,7 +44,8 @@ def host():
 class TtgOpInfo(ctypes.Structure):
     _fields_ = [("n", c_i64), ("nnz_h", c_i64), ("nnz_c", c_i64), ("nproj", c_i32),
                 ("group_rows", c_i32), ("n_groups", c_i64), ("stored_cols", c_i64),
-                ("fill", c_dbl), ("device_bytes", c_i64), ("launches", c_i64)]
+                ("fill", c_dbl), ("device_bytes", c_i64), ("launches", c_i64),
+                ("n_tiles", c_i64), ("tile_slots", c_i64), ("tile_fill", c_dbl)]
 
 
 class TtgSched(ctypes.Structure):
@@ -55,7 +56,10 @@ class TtgSched(ctypes.Structure):
 _SIGS = {
     "ttg_device_query": [c_vp, c_vp, c_vp],
     "ttg_op_create": [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp],
+    "ttg_op_create_tucker": [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32,
+                             c_vp],
     "ttg_op_destroy": [c_vp],
+    "ttg_op_set_rr_precision": [c_vp, c_i32],
     "ttg_op_info": [c_vp, c_vp],
     "ttg_op_sync": [c_vp],
     "ttg_op_record": [c_vp, c_i32],
@@ -78,11 +82,22 @@ _SIGS = {
     "ttg_lanczos_bounds": [c_vp, c_vp, c_i32, c_vp, c_vp],
     "ttg_chfsi_pass": [c_vp, c_vp, c_i32, c_dbl, c_dbl, c_dbl, TtgSched, c_i32, c_vp],
     "ttg_fermi": [c_vp, c_i32, c_vp, c_dbl, c_dbl, c_i32, c_vp, c_vp],
+    "ttg_op_set_kinetic": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
+    "ttg_op_update_potential": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
+    "ttg_tucker_sthosvd": [c_vp, c_vp, c_vp, c_dbl, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
+    "ttg_tucker_reconstruct": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
+    "ttg_grid_lda": [c_vp, c_i64, c_vp, c_vp, c_i32, c_vp],
+    "ttg_grid_integrate": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
+    "ttg_grid_lincomb": [c_i32, c_vp, c_vp, c_i64, c_vp, c_i32, c_vp],
+    "ttg_grid_cp_sum": [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp],
+    "ttg_grid_ion_potential": [c_i32, c_vp, c_vp, c_dbl, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
     "ttg_density": [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp,
                     c_vp, c_vp],
     "ttg_hartree": [c_i32, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_i32, c_i32, c_i32,
                     c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32,
                     c_vp, c_vp, c_vp, c_vp, c_vp],
+    "ttg_hartree_energy": [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                           c_vp, c_vp, c_vp, c_vp, c_vp],
 }
 _OTHER = {
     "ttg_version": ([], ctypes.c_char_p),

@@ -27,7 +27,7 @@ from . import _lib
 from ._lib import TtgSched, check, ptr
 from .system import Csr
 
-PREC = {"fp64": 0, "fp32": 1, "bf16": 2}
+PREC = {"fp64": 0, "fp32": 1, "bf16": 2, "df64": 3}
 
 
 def sched(high="fp32", low=None, n_low=0, return_prev=False) -> TtgSched:
@@ -44,8 +44,10 @@ class ProjectHamiltonianSparse:
     The reference stores C_nloc = diag(D) C and C_nloc_trans = C^T
     (dft/ProjectHamiltonianSparse.cc:316-325); both are views of (C, D) here."""
 
-    def __init__(self, H_loc: Csr, C: Csr | None = None, D: np.ndarray | None = None):
+    def __init__(self, H_loc: Csr, C: Csr | None = None, D: np.ndarray | None = None,
+                 ranks: tuple | None = None):
         self.H_loc = H_loc
+        self.ranks = ranks          # Tucker ranks (rx, ry, rz) of the basis, if known
         if C is None:
             C = Csr(0, H_loc.n_cols, np.zeros(1, np.int64), np.zeros(0, np.int32), np.zeros(0))
             D = np.zeros(0)
@@ -62,7 +64,7 @@ class ProjectHamiltonianSparse:
 
     @classmethod
     def from_system(cls, s) -> "ProjectHamiltonianSparse":
-        return cls(s.H, s.C, s.D)
+        return cls(s.H, s.C, s.D, tuple(b.r for b in s.basis))
 
 
 class Operator:
@@ -78,16 +80,21 @@ class Operator:
         hp = hp.astype(np.int64, copy=False)
         cp = cp.astype(np.int64, copy=False)
         handle = ctypes.c_void_p()
-        check(lib.ttg_op_create(h.n_rows, ptr(hp), ptr(hc.astype(np.int32, copy=False)),
-                                ptr(hv.astype(np.float64, copy=False)), c.n_rows, ptr(cp),
-                                ptr(cc.astype(np.int32, copy=False)),
-                                ptr(cv.astype(np.float64, copy=False)), ptr(d), int(max_k),
-                                ctypes.byref(handle)), "ttg_op_create")
+        ranks = None if H.ranks is None else np.array(H.ranks, dtype=np.int32)
+        check(lib.ttg_op_create_tucker(h.n_rows, ptr(hp), ptr(hc.astype(np.int32, copy=False)),
+                                       ptr(hv.astype(np.float64, copy=False)), c.n_rows, ptr(cp),
+                                       ptr(cc.astype(np.int32, copy=False)),
+                                       ptr(cv.astype(np.float64, copy=False)), ptr(d), ptr(ranks),
+                                       int(max_k), ctypes.byref(handle)), "ttg_op_create_tucker")
         self.h = handle
         self.n = h.n_rows
         self.max_k = max_k
         self._keep = None
         self._blocks = weakref.WeakSet()
+
+    def set_rr_precision(self, prec: str):
+        """Arithmetic of H X in Rayleigh-Ritz: "df64" (default) or "fp64"."""
+        check(_lib.ttg().ttg_op_set_rr_precision(self.h, PREC[prec]), "ttg_op_set_rr_precision")
 
     def info(self) -> dict:
         inf = _lib.TtgOpInfo()
@@ -301,3 +308,24 @@ def hartree(alpha, omega, G, quad, Uq, grids):
                                  ptr(g[0]), ptr(g[1]), ptr(g[2]), ptr(V), ctypes.byref(ms)),
           "ttg_hartree")
     return V.reshape(nz, ny, nx), ms.value
+
+
+def hartree_energy(alpha, omega, G, quad, Uq):
+    """1/2 int rho V_H(rho) of a Tucker density on its quadrature grid, FP64
+    (see include/ttg.h: ttg_hartree_energy).  G: (rz, ry, rx); quad and Uq as
+    for hartree()."""
+    alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+    omega = np.ascontiguousarray(omega, dtype=np.float64)
+    G = np.ascontiguousarray(G, dtype=np.float64)
+    rz, ry, rx = G.shape
+    q = [(np.ascontiguousarray(a, np.float64), np.ascontiguousarray(w, np.float64)) for a, w in quad]
+    U = [np.asfortranarray(u, dtype=np.float64) for u in Uq]
+    ranks = np.array([rx, ry, rz], np.int32)
+    nq = np.array([q[d][0].size for d in range(3)], np.int32)
+    e = ctypes.c_double()
+    check(_lib.ttg().ttg_hartree_energy(alpha.size, ptr(alpha), ptr(omega), ptr(ranks), ptr(G),
+                                        ptr(nq), ptr(q[0][0]), ptr(q[1][0]), ptr(q[2][0]),
+                                        ptr(q[0][1]), ptr(q[1][1]), ptr(q[2][1]),
+                                        ptr(U[0]), ptr(U[1]), ptr(U[2]), ctypes.byref(e)),
+          "ttg_hartree_energy")
+    return e.value

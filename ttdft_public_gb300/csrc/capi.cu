@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <utility>
 #include <vector>
@@ -84,8 +85,18 @@ ttg_status ttg_op_create(int64_t n, const int64_t* h_row_ptr, const int32_t* h_c
                          const double* h_val, int32_t nproj, const int64_t* c_row_ptr,
                          const int32_t* c_col, const double* c_val, const double* d,
                          int32_t max_k, ttg_op** out) {
+  return ttg_op_create_tucker(n, h_row_ptr, h_col, h_val, nproj, c_row_ptr, c_col, c_val, d,
+                              nullptr, max_k, out);
+}
+
+ttg_status ttg_op_create_tucker(int64_t n, const int64_t* h_row_ptr, const int32_t* h_col,
+                                const double* h_val, int32_t nproj, const int64_t* c_row_ptr,
+                                const int32_t* c_col, const double* c_val, const double* d,
+                                const int32_t* tucker_ranks, int32_t max_k, ttg_op** out) {
   if (!out || n <= 0 || n > INT32_MAX - 65536 || nproj < 0 || nproj > 65536 || max_k <= 0 ||
       max_k > 4096 || !h_row_ptr)
+    return TTG_BAD_ARG;
+  if (tucker_ranks && (int64_t)tucker_ranks[0] * tucker_ranks[1] * tucker_ranks[2] != n)
     return TTG_BAD_ARG;
   *out = nullptr;
   int32_t smc, ma, mi;
@@ -96,6 +107,9 @@ ttg_status ttg_op_create(int64_t n, const int64_t* h_row_ptr, const int32_t* h_c
   op->nproj = nproj;
   op->max_k = max_k;
   op->ld = round_up(max_k, 8);
+  op->keep_pattern = tucker_ranks != nullptr;
+  if (tucker_ranks)
+    for (int d = 0; d < 3; ++d) op->pattern.r[d] = tucker_ranks[d];
   auto fail = [&](ttg_status s) {
     ttg_op_destroy(op);
     return s;
@@ -107,10 +121,17 @@ ttg_status ttg_op_create(int64_t n, const int64_t* h_row_ptr, const int32_t* h_c
   ttg_status s = build_row_groups(op, n, h_row_ptr, h_col, h_val, nproj, c_row_ptr, c_col,
                                   c_val, d);
   if (s != TTG_OK) return fail(s);
+  const char* dis = getenv("TTG_DISABLE_TC");
+  op->tc_disabled = dis && dis[0] == '1';
+  if (!op->tc_disabled) {
+    s = build_tiles(op, n, h_row_ptr, h_col, h_val, nproj, c_row_ptr, c_col, c_val, tucker_ranks);
+    if (s != TTG_OK) return fail(s);
+  }
   const int64_t kmax = std::max<int64_t>(max_k, kMaxLanczos);
   if ((s = ensure(op->kk0, kmax * kmax * 8, op)) != TTG_OK) return fail(s);
   if ((s = ensure(op->kk1, kmax * kmax * 8, op)) != TTG_OK) return fail(s);
   if ((s = ensure(op->kk2, kmax * kmax * 8, op)) != TTG_OK) return fail(s);
+  if ((s = ensure(op->kk3, (kmax * kmax + 6 * kmax + 64) * 8, op)) != TTG_OK) return fail(s);
   if ((s = ensure(op->scal, (kScalJacobi + 4 * (kmax + 2) + kmax) * 8, op)) != TTG_OK)
     return fail(s);
   if ((s = ensure(op->status, 64, op)) != TTG_OK) return fail(s);
@@ -125,9 +146,14 @@ ttg_status ttg_op_destroy(ttg_op* op) {
   if (!op) return TTG_BAD_ARG;
   if (op->stream) cudaStreamSynchronize(op->stream);
   DevBuf* bufs[] = {&op->rg.gptr, &op->rg.gcol, &op->rg.v64, &op->rg.v32, &op->rg.v16,
+                    &op->rg.vdf,  &op->wdf,     &op->wpart,
                     &op->C.ptr,   &op->C.col,   &op->C.val,  &op->C.val32, &op->w32a,
                     &op->w32b,    &op->w16a,    &op->w16b,   &op->w64,     &op->kk0,
-                    &op->kk1,     &op->kk2,     &op->partial, &op->scal,   &op->status};
+                    &op->kk1,     &op->kk2,     &op->kk3,     &op->eigbuf,  &op->eigf,    &op->partial, &op->scal,   &op->status,
+                    &op->tiles.tptr, &op->tiles.tcol, &op->tiles.rowmap, &op->tiles.v32,
+                    &op->tiles.v16, &op->pattern.row_ptr, &op->pattern.col,
+                    &op->pattern.rg_pos, &op->pattern.tile_base, &op->pattern.tile_slot,
+                    &op->pattern.kin, &op->pattern.work, &op->pattern.work2};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < kMaxSlots; ++i)
     if (op->ev[i]) cudaEventDestroy(op->ev[i]);
@@ -150,10 +176,21 @@ ttg_status ttg_op_info(const ttg_op* op, ttg_op_info_t* info) {
                    : 0.0;
   info->device_bytes = op->device_bytes;
   info->launches = op->launches;
+  info->n_tiles = op->tiles.n_tiles;
+  info->tile_slots = op->tiles.slots;
+  info->tile_fill = op->tiles.slots > 0
+                        ? (double)(op->nnz_h + op->nnz_c) / (64.0 * op->tiles.slots)
+                        : 0.0;
   return TTG_OK;
 }
 
 void* ttg_op_stream(ttg_op* op) { return op ? (void*)op->stream : nullptr; }
+
+ttg_status ttg_op_set_rr_precision(ttg_op* op, int32_t prec) {
+  if (!op || (prec != TTG_PREC_FP64 && prec != TTG_PREC_DF64)) return TTG_BAD_ARG;
+  op->rr_prec = prec;
+  return TTG_OK;
+}
 
 ttg_status ttg_op_sync(ttg_op* op) {
   if (!op) return TTG_BAD_ARG;
@@ -371,7 +408,7 @@ ttg_status ttg_chol_qr(ttg_op* op, ttg_block* X) {
 }
 
 static ttg_status eig_device(ttg_op* op, int k, double* A, double* V, double* w_dev) {
-  TTG_TRY(syev_jacobi(op, A, V, w_dev, k, op->status.as<int>()));
+  TTG_TRY(syev_device(op, A, V, w_dev, k, op->status.as<int>()));
   int st = 0;
   TTG_TRY(read_status(op, &st));
   return st == 0 ? TTG_OK : TTG_NOT_CONVERGED;
@@ -401,9 +438,12 @@ ttg_status ttg_rayleigh_ritz(ttg_op* op, ttg_block* X, int32_t rotate, double* w
                              double* q_host) {
   TTG_TRY(check_block(op, X));
   const int k = X->k;
-  // HX into w64 (FP64), then P = X^T HX
+  // HX into w64 (FP64 values), then P = X^T HX
   TTG_TRY(launch_proj_w(op, TTG_PREC_FP64, X->x.p, k));
-  TTG_TRY(launch_cheb_step(op, TTG_PREC_FP64, X->x.p, nullptr, op->w64.p, k, 1.0, 0.0, 0.0));
+  if (op->rr_prec == TTG_PREC_DF64)
+    TTG_TRY(launch_apply_df64(op, X->x.as<double>(), op->w64.as<double>(), k));
+  else
+    TTG_TRY(launch_cheb_step(op, TTG_PREC_FP64, X->x.p, nullptr, op->w64.p, k, 1.0, 0.0, 0.0));
   TTG_TRY(gram_tn(op, X->x.as<double>(), op->w64.as<double>(), k, op->kk0.as<double>()));
   double* wdev = op->scal.as<double>() + kScalEig;
   TTG_TRY(eig_device(op, k, op->kk0.as<double>(), op->kk1.as<double>(), wdev));

@@ -9,10 +9,11 @@
 //                  variant :309-404).
 //   cholesky_inv   S = L L^T and L^-1, status on a non-positive pivot
 //                  (the reference ignores potrf's info, MultTm.cu:283-294).
-//   syev_jacobi    symmetric eigensolver (cyclic Jacobi, round-robin pair
-//                  ordering, all disjoint rotations of a round in parallel),
-//                  ascending eigenvalues; replaces the SLEPc/LAPACK call of
-//                  EigenSolver::computeEigenPairsSeq (EigenSolver.cc:30-184).
+//   syev_device    symmetric eigensolver: Householder tridiagonalisation +
+//                  implicit QL in FP32, then FP64 iterative refinement
+//                  (Ogita-Aishima); ascending eigenvalues.  Replaces the
+//                  SLEPc/LAPACK call of EigenSolver::computeEigenPairsSeq
+//                  (EigenSolver.cc:30-184).
 //   lanczos_step   one Lanczos three-term step on the device
 //                  (EigenSolver.cc:262-315).
 //   fermi          Newton iteration for the Fermi level
@@ -136,13 +137,14 @@ __global__ void __launch_bounds__(256) k_gemm_nn(const double* __restrict__ X,
     }
 }
 
-__device__ double block_sum(double v, double* red) {
+template <typename T>
+__device__ T block_sum(T v, T* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int w = threadIdx.x / 32, l = threadIdx.x % 32;
   __syncthreads();
   if (l == 0) red[w] = v;
   __syncthreads();
-  double s = 0.0;
+  T s = T(0);
   const int nw = (blockDim.x + 31) / 32;
   for (int i = 0; i < nw; ++i) s += red[i];
   return s;
@@ -202,96 +204,313 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv(double* A, double* Linv, 
   }
 }
 
-// Cyclic Jacobi on a symmetric k x k column-major A (overwritten), V = eigvecs.
-// One CTA.  status[0]: 0 converged, 1 not converged within max_sweeps.
-__global__ void __launch_bounds__(1024) k_jacobi(double* A, double* V, double* w, int k,
-                                                 int max_sweeps, double tol, int* status,
-                                                 double* cs_buf) {
-  __shared__ double red[32];
-  const int m = (k % 2 == 0) ? k : k + 1;      // players incl. a dummy
-  const int npairs = m / 2;
-  double* cs = cs_buf;                          // [npairs][2]
-  int* pq = reinterpret_cast<int*>(cs_buf + 2 * npairs);
-  for (int64_t e = threadIdx.x; e < (int64_t)k * k; e += blockDim.x) {
-    const int i = (int)(e % k), j = (int)(e / k);
-    V[e] = (i == j) ? 1.0 : 0.0;
+// Symmetric eigensolver in two stages, one CTA, FP64:
+//  (1) Householder reduction to tridiagonal form, A = Q T Q^T: for each
+//      column j, v = x - alpha e1 with x = A[j+1:, j], P = I - tau v v^T and
+//      the trailing block is updated as B <- P B P = B - v w^T - w v^T with
+//      p = tau B v, w = p - (tau/2)(v.p) v; Q accumulates the reflectors.
+//  (2) implicit QL iterations with Wilkinson-type shifts on T (the classical
+//      tql algorithm), one thread running the scalar recurrence and storing
+//      each sweep's plane rotations, all threads then applying them to their
+//      own rows of Q.
+// 4n^3/3 flops for (1) plus O(n^2) rotations on Q in (2), against ~10
+// sweeps of 3n^3 for Jacobi.  status[0]: 0 ok, 1 QL did not converge.
+template <typename T, bool DO_QL = true>
+__global__ void __launch_bounds__(1024) k_tridiag_ql(T* A, T* Q, T* w, int n, int* status,
+                                                     T* scratch) {
+  const T kTiny = sizeof(T) == 4 ? T(1.2e-7) : T(1e-16);
+  __shared__ T red[32];
+  __shared__ T s_alpha, s_tau;
+  T* v = scratch;               // n
+  T* p = scratch + n;           // n
+  T* d = scratch + 2 * n;       // n
+  T* e = scratch + 3 * n;       // n
+  T* vs = scratch + 4 * n;      // n*n: reflectors, column j holds v_j (rows j+1..)
+  T* rot = vs + (int64_t)n * n; // 2n: (c, s) of one QL sweep
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // ---- (1) tridiagonalisation
+  for (int j = 0; j + 2 < n; ++j) {
+    const int m = n - j - 1;
+    T ss = 0.0;
+    for (int r = tid; r < m; r += nt) {
+      const T x = A[(j + 1 + r) + (int64_t)j * n];
+      ss += x * x;
+    }
+    ss = block_sum(ss, red);
+    if (tid == 0) {
+      const T x0 = A[(j + 1) + (int64_t)j * n];
+      const T nrm = sqrt(ss);
+      const T alpha = x0 >= 0 ? -nrm : nrm;
+      const T vnorm2 = ss - x0 * x0 + (x0 - alpha) * (x0 - alpha);
+      s_alpha = alpha;
+      s_tau = vnorm2 > T(0) ? T(2) / vnorm2 : T(0);
+    }
+    __syncthreads();
+    const T alpha = s_alpha, tau = s_tau;
+    for (int r = tid; r < m; r += nt) {
+      const T x = A[(j + 1 + r) + (int64_t)j * n];
+      const T vr = (r == 0) ? x - alpha : x;
+      v[r] = vr;
+      vs[(j + 1 + r) + (int64_t)j * n] = vr;
+    }
+    __syncthreads();
+    if (tau == T(0)) continue;
+    // p = tau B v  (B = A[j+1:, j+1:], column-major)
+    for (int r = tid; r < m; r += nt) {
+      T acc = 0.0;
+      for (int c = 0; c < m; ++c) acc += A[(j + 1 + r) + (int64_t)(j + 1 + c) * n] * v[c];
+      p[r] = tau * acc;
+    }
+    __syncthreads();
+    T vp = 0.0;
+    for (int r = tid; r < m; r += nt) vp += v[r] * p[r];
+    vp = block_sum(vp, red);
+    const T K = T(0.5) * tau * vp;
+    for (int r = tid; r < m; r += nt) p[r] -= K * v[r];   // p becomes w
+    __syncthreads();
+    for (int64_t e2 = tid; e2 < (int64_t)m * m; e2 += nt) {
+      const int r = (int)(e2 % m), c = (int)(e2 / m);
+      A[(j + 1 + r) + (int64_t)(j + 1 + c) * n] -= v[r] * p[c] + p[r] * v[c];
+    }
+    if (tid == 0) {
+      A[(j + 1) + (int64_t)j * n] = alpha;
+      A[j + (int64_t)(j + 1) * n] = alpha;
+    }
+    __syncthreads();
   }
-  // Frobenius norm for the stopping test
-  double loc = 0.0;
-  for (int64_t e = threadIdx.x; e < (int64_t)k * k; e += blockDim.x) loc += A[e] * A[e];
-  const double fro2 = block_sum(loc, red);
-  int converged = 0;
-  int sweep = 0;
-  for (; sweep < max_sweeps; ++sweep) {
-    double off = 0.0;
-    for (int64_t e = threadIdx.x; e < (int64_t)k * k; e += blockDim.x) {
-      const int i = (int)(e % k), j = (int)(e / k);
-      if (i != j) off += A[e] * A[e];
+  for (int i = tid; i < n; i += nt) {
+    d[i] = A[i + (int64_t)i * n];
+    e[i] = (i + 1 < n) ? A[(i + 1) + (int64_t)i * n] : 0.0;
+  }
+  // Q = P_0 P_1 ... P_{n-3}, built backwards: Q <- P_j Q on rows/cols j+1..
+  for (int64_t e2 = tid; e2 < (int64_t)n * n; e2 += nt) {
+    const int r = (int)(e2 % n), c = (int)(e2 / n);
+    Q[e2] = (r == c) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  for (int j = n - 3; j >= 0; --j) {
+    const int m = n - j - 1;
+    T vn = 0.0;
+    for (int r = tid; r < m; r += nt) {
+      const T x = vs[(j + 1 + r) + (int64_t)j * n];
+      vn += x * x;
     }
-    off = block_sum(off, red);
-    // rounding leaves off-diagonal entries of order eps*|A|, so the threshold
-    // grows with k: (tol^2 * k) * |A|_F^2
-    if (off <= tol * tol * (double)k * fro2 || off == 0.0) {
-      converged = 1;
-      break;
+    vn = block_sum(vn, red);
+    if (vn == T(0)) continue;
+    const T tau = T(2) / vn;
+    // columns c of the trailing block: Q[:, c] -= tau v (v . Q[:, c])
+    for (int c = tid; c < m; c += nt) {
+      T dot = 0.0;
+      for (int r = 0; r < m; ++r)
+        dot += vs[(j + 1 + r) + (int64_t)j * n] * Q[(j + 1 + r) + (int64_t)(j + 1 + c) * n];
+      p[c] = tau * dot;
     }
-    for (int r = 0; r < m - 1; ++r) {
-      // pairs of this round: player 0 fixed, the others rotate
-      for (int i = threadIdx.x; i < npairs; i += blockDim.x) {
-        const int a = (i == 0) ? 0 : 1 + ((i - 1 + r) % (m - 1));
-        const int bj = m - 1 - i;
-        const int b = 1 + ((bj - 1 + r) % (m - 1));
-        int p = min(a, b), q = max(a, b);
-        double c = 1.0, s = 0.0;
-        if (q < k) {
-          const double apq = A[p + (int64_t)q * k];
-          if (apq != 0.0) {
-            const double app = A[p + (int64_t)p * k], aqq = A[q + (int64_t)q * k];
-            const double theta = (aqq - app) / (2.0 * apq);
-            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
-            c = 1.0 / sqrt(1.0 + t * t);
-            s = t * c;
-          }
-        } else {
-          q = -1;
+    __syncthreads();
+    for (int64_t e2 = tid; e2 < (int64_t)m * m; e2 += nt) {
+      const int r = (int)(e2 % m), c = (int)(e2 / m);
+      Q[(j + 1 + r) + (int64_t)(j + 1 + c) * n] -= vs[(j + 1 + r) + (int64_t)j * n] * p[c];
+    }
+    __syncthreads();
+  }
+  if constexpr (!DO_QL) {
+    if (tid == 0) status[0] = 0;
+    return;
+  }
+  // ---- (2) implicit QL on (d, e), rotations applied to the rows of Q
+  __shared__ int s_m, s_done, s_fail, s_nrot;
+  __shared__ T s_floor;
+  if (tid == 0) {
+    s_fail = 0;
+    T tn = T(0);
+    for (int i = 0; i < n; ++i) tn = fmax(tn, fabs(d[i]) + fabs(e[i]));
+    // off-diagonals below kTiny^2 |T| are zero at this precision
+    s_floor = kTiny * kTiny * tn;
+  }
+  __syncthreads();
+  for (int l = 0; l < n; ++l) {
+    int iter = 0;
+    while (true) {
+      if (tid == 0) {
+        int m = l;
+        for (; m < n - 1; ++m) {
+          const T dd = fabs(d[m]) + fabs(d[m + 1]);
+          if (fabs(e[m]) <= kTiny * dd || fabs(e[m]) <= s_floor) break;
         }
-        cs[2 * i] = c;
-        cs[2 * i + 1] = s;
-        pq[2 * i] = p;
-        pq[2 * i + 1] = q;
+        s_m = m;
+        s_done = (m == l);
+        s_nrot = 0;
+        if (!s_done) {
+          if (++iter > 100) {
+            s_fail = 1;
+            s_done = 1;
+          } else {
+            T g = (d[l + 1] - d[l]) / (T(2) * e[l]);
+            T r = hypot(g, T(1));
+            g = d[m] - d[l] + e[l] / (g + (g >= 0 ? fabs(r) : -fabs(r)));
+            T s = T(1), c = T(1), pp = T(0);
+            int i = m - 1;
+            bool underflow = false;
+            for (; i >= l; --i) {
+              const T f = s * e[i], b = c * e[i];
+              r = hypot(f, g);
+              e[i + 1] = r;
+              if (r == T(0)) {
+                d[i + 1] -= pp;
+                e[m] = T(0);
+                underflow = true;
+                break;
+              }
+              s = f / r;
+              c = g / r;
+              g = d[i + 1] - pp;
+              r = (d[i] - g) * s + T(2) * c * b;
+              pp = s * r;
+              d[i + 1] = g + pp;
+              g = c * r - b;
+              rot[2 * s_nrot] = c;
+              rot[2 * s_nrot + 1] = s;
+              s_nrot++;
+            }
+            if (!underflow) {
+              d[l] -= pp;
+              e[l] = g;
+              e[m] = T(0);
+            }
+          }
+        }
       }
       __syncthreads();
-      // rows: A <- J^T A
-      for (int64_t e = threadIdx.x; e < (int64_t)npairs * k; e += blockDim.x) {
-        const int i = (int)(e / k), j = (int)(e % k);
-        const int p = pq[2 * i], q = pq[2 * i + 1];
-        if (q < 0) continue;
-        const double c = cs[2 * i], s = cs[2 * i + 1];
-        if (s == 0.0) continue;
-        const double ap = A[p + (int64_t)j * k], aq = A[q + (int64_t)j * k];
-        A[p + (int64_t)j * k] = c * ap - s * aq;
-        A[q + (int64_t)j * k] = s * ap + c * aq;
-      }
-      __syncthreads();
-      // columns: A <- A J, V <- V J
-      for (int64_t e = threadIdx.x; e < (int64_t)npairs * k; e += blockDim.x) {
-        const int i = (int)(e / k), j = (int)(e % k);
-        const int p = pq[2 * i], q = pq[2 * i + 1];
-        if (q < 0) continue;
-        const double c = cs[2 * i], s = cs[2 * i + 1];
-        if (s == 0.0) continue;
-        const double ap = A[j + (int64_t)p * k], aq = A[j + (int64_t)q * k];
-        A[j + (int64_t)p * k] = c * ap - s * aq;
-        A[j + (int64_t)q * k] = s * ap + c * aq;
-        const double vp = V[j + (int64_t)p * k], vq = V[j + (int64_t)q * k];
-        V[j + (int64_t)p * k] = c * vp - s * vq;
-        V[j + (int64_t)q * k] = s * vp + c * vq;
+      if (s_done) break;
+      // rotation q (i = m-1-q) mixes columns i and i+1 of Q, for every row
+      const int m = s_m, nr = s_nrot;
+      for (int row = tid; row < n; row += nt) {
+        for (int q = 0; q < nr; ++q) {
+          const int i = m - 1 - q;
+          const T c = rot[2 * q], s = rot[2 * q + 1];
+          const T f = Q[row + (int64_t)(i + 1) * n];
+          const T zi = Q[row + (int64_t)i * n];
+          Q[row + (int64_t)(i + 1) * n] = s * zi + c * f;
+          Q[row + (int64_t)i * n] = c * zi - s * f;
+        }
       }
       __syncthreads();
     }
+    if (s_fail) break;
   }
-  for (int i = threadIdx.x; i < k; i += blockDim.x) w[i] = A[i + (int64_t)i * k];
-  if (threadIdx.x == 0) status[0] = converged ? 0 : 1;
+  for (int i = tid; i < n; i += nt) w[i] = d[i];
+  if (tid == 0) status[0] = s_fail;
+}
+
+// Largest r eigenpairs of a symmetric tridiagonal T (d, e: e[i] couples i and
+// i+1), FP64, one CTA.  Eigenvalues by bisection on Sturm counts, one thread
+// per eigenvalue, to full FP64 resolution (Gershgorin start interval);
+// eigenvectors by two steps of inverse iteration with a tridiagonal LU
+// (partial pivoting), then modified Gram-Schmidt in index order, which
+// separates the vectors of close eigenvalues.  Z is n x r column-major, w
+// descending.  Work space per thread: 4n doubles in `work`.
+__global__ void __launch_bounds__(256) k_tridiag_topk(const double* __restrict__ d,
+                                                      const double* __restrict__ e, int n, int r,
+                                                      double* __restrict__ w, double* Z,
+                                                      double* work) {
+  __shared__ double red[32];
+  __shared__ double s_lo, s_hi;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    double lo = 1e300, hi = -1e300;
+    for (int i = 0; i < n; ++i) {
+      const double rad = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
+      lo = fmin(lo, d[i] - rad);
+      hi = fmax(hi, d[i] + rad);
+    }
+    const double pad = 1e-14 * fmax(fabs(lo), fabs(hi)) + 1e-300;
+    s_lo = lo - pad;
+    s_hi = hi + pad;
+  }
+  __syncthreads();
+  const double tnorm = fmax(fabs(s_lo), fabs(s_hi));
+  const double tiny = 1e-300;
+  for (int j = tid; j < r; j += blockDim.x) {
+    // eigenvalue index (ascending) n-1-j: count(x) = #eigenvalues < x
+    const int target = n - 1 - j;
+    double lo = s_lo, hi = s_hi;
+    for (int it = 0; it < 200 && hi - lo > 2.2e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300; ++it) {
+      const double x = 0.5 * (lo + hi);
+      int cnt = 0;
+      double q = d[0] - x;
+      if (q < 0) ++cnt;
+      for (int i = 1; i < n; ++i) {
+        if (fabs(q) < tiny) q = -tiny;
+        q = d[i] - x - e[i - 1] * e[i - 1] / q;
+        if (q < 0) ++cnt;
+      }
+      if (cnt > target) hi = x; else lo = x;
+    }
+    const double lam = 0.5 * (lo + hi);
+    w[j] = lam;
+    // inverse iteration: (T - lam I) z = b, LU with partial pivoting
+    double* dg = work + (int64_t)j * 4 * n;      // diagonal of U
+    double* u1 = dg + n;                         // first superdiagonal of U
+    double* u2 = u1 + n;                         // second superdiagonal (from pivoting)
+    double* z = u2 + n;                          // rhs / solution
+    for (int i = 0; i < n; ++i) z[i] = 1.0 / sqrt((double)n) * (1.0 + 0.01 * ((i * 7 + j * 13) % 17));
+    const double shift_guard = 1e-15 * tnorm + 1e-300;
+    for (int pass = 0; pass < 3; ++pass) {
+      // factor (T - lam I) = P L U, rows processed top-down; b transformed on the fly
+      double a = d[0] - lam, b = (n > 1 ? e[0] : 0.0), c = 0.0;   // current row: a, b, c
+      double zc = z[0];
+      for (int i = 0; i + 1 < n; ++i) {
+        const double sub = e[i];                 // T[i+1][i]
+        const double na = d[i + 1] - lam, nb = (i + 2 < n ? e[i + 1] : 0.0);
+        double zn = z[i + 1];
+        if (fabs(a) >= fabs(sub)) {
+          const double m = (fabs(a) > 0 ? sub / a : 0.0);
+          dg[i] = a; u1[i] = b; u2[i] = c;
+          a = na - m * b; b = nb - m * c; c = 0.0;
+          zn -= m * zc;
+        } else {
+          const double m = a / sub;              // swap rows i and i+1
+          dg[i] = sub; u1[i] = na; u2[i] = nb;
+          const double t = zc; zc = zn; zn = t - m * zn;
+          a = b - m * na; b = c - m * nb; c = 0.0;
+        }
+        z[i] = zc;
+        zc = zn;
+      }
+      dg[n - 1] = a;
+      z[n - 1] = zc;
+      // back substitution
+      for (int i = n - 1; i >= 0; --i) {
+        double v = z[i];
+        if (i + 1 < n) v -= u1[i] * z[i + 1];
+        if (i + 2 < n) v -= u2[i] * z[i + 2];
+        const double piv = fabs(dg[i]) > shift_guard ? dg[i] : (dg[i] >= 0 ? shift_guard : -shift_guard);
+        z[i] = v / piv;
+      }
+      double nrm = 0.0;
+      for (int i = 0; i < n; ++i) nrm += z[i] * z[i];
+      nrm = 1.0 / sqrt(nrm);
+      for (int i = 0; i < n; ++i) z[i] *= nrm;
+    }
+  }
+  __syncthreads();
+  // modified Gram-Schmidt over the r vectors in index order (block-parallel)
+  for (int j = 0; j < r; ++j) {
+    double* zj = work + (int64_t)j * 4 * n + 3 * n;
+    for (int i2 = 0; i2 < j; ++i2) {
+      const double* zi = Z + (int64_t)i2 * n;
+      double dot = 0.0;
+      for (int t = tid; t < n; t += blockDim.x) dot += zi[t] * zj[t];
+      dot = block_sum(dot, red);
+      for (int t = tid; t < n; t += blockDim.x) zj[t] -= dot * zi[t];
+      __syncthreads();
+    }
+    double nn = 0.0;
+    for (int t = tid; t < n; t += blockDim.x) nn += zj[t] * zj[t];
+    nn = block_sum(nn, red);
+    const double inv = 1.0 / sqrt(nn);
+    for (int t = tid; t < n; t += blockDim.x) Z[(int64_t)j * n + t] = zj[t] * inv;
+    __syncthreads();
+  }
 }
 
 // Sort eigenpairs ascending (stable rank sort), normalise each eigenvector's
@@ -312,6 +531,64 @@ __global__ void k_sort_eig(const double* w, const double* V, double* w_out, doub
     const double sg = V[ib + (int64_t)j * k] < 0 ? -1.0 : 1.0;
     for (int i = 0; i < k; ++i) V_out[i + (int64_t)rank * k] = sg * V[i + (int64_t)j * k];
   }
+}
+
+// One step of the Ogita-Aishima iterative refinement of a symmetric
+// eigendecomposition (Ogita & Aishima, Japan J. Indust. Appl. Math. 35 (2018)):
+// with G = V^T V, S = V^T A V, r_ij = delta_ij - G_ij, lam_i = S_ii / G_ii,
+// delta = 2 (|S - diag(lam)| + |A| |R|) (Frobenius norms, bounds of the 2-norms),
+// E_ij = (S_ij + lam_j r_ij) / (lam_j - lam_i) if |lam_i - lam_j| > delta, else r_ij / 2;
+// the caller then forms V <- V + V E.  One CTA.
+__global__ void __launch_bounds__(1024) k_oa_step(const double* __restrict__ G,
+                                                  const double* __restrict__ S, int k,
+                                                  const double* __restrict__ normA, double* E,
+                                                  double* lam) {
+  __shared__ double red[32];
+  for (int i = threadIdx.x; i < k; i += blockDim.x) lam[i] = S[i + (int64_t)i * k] / G[i + (int64_t)i * k];
+  __syncthreads();
+  double sd = 0.0, rr = 0.0;
+  for (int64_t e = threadIdx.x; e < (int64_t)k * k; e += blockDim.x) {
+    const int i = (int)(e % k), j = (int)(e / k);
+    const double sij = S[e] - (i == j ? lam[i] : 0.0);
+    const double rij = (i == j ? 1.0 : 0.0) - G[e];
+    sd += sij * sij;
+    rr += rij * rij;
+  }
+  sd = block_sum(sd, red);
+  rr = block_sum(rr, red);
+  const double delta = 2.0 * (sqrt(sd) + sqrt(*normA) * sqrt(rr));
+  for (int64_t e = threadIdx.x; e < (int64_t)k * k; e += blockDim.x) {
+    const int i = (int)(e % k), j = (int)(e / k);
+    const double rij = (i == j ? 1.0 : 0.0) - G[e];
+    const double gap = lam[j] - lam[i];
+    E[e] = fabs(gap) > delta ? (S[e] + lam[j] * rij) / gap : 0.5 * rij;
+  }
+}
+
+__global__ void k_frob2(const double* __restrict__ A, int64_t n, double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) s += A[e] * A[e];
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) *out = s;
+}
+
+__global__ void k_add(double* __restrict__ a, const double* __restrict__ b, int64_t n) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    a[e] += b[e];
+}
+
+__global__ void k_d2f_vec(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    b[e] = (float)a[e];
+}
+
+__global__ void k_f2d_vec(const float* __restrict__ a, double* __restrict__ b, int64_t n) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    b[e] = (double)a[e];
 }
 
 __global__ void k_symmetrize(double* A, int k) {
@@ -483,21 +760,87 @@ ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_statu
   return TTG_OK;
 }
 
-ttg_status syev_jacobi(ttg_op* op, double* A, double* V, double* w, int k, int* d_status) {
-  // scratch layout in op->scal (doubles): [kScalJacobi, +4(k+2)) rotations and
-  // pair ids, then k unsorted eigenvalues.  Unsorted eigenvectors go to kk2.
-  const int64_t need = (kScalJacobi + 4 * (int64_t)(k + 2) + k) * (int64_t)sizeof(double);
-  if ((int64_t)op->scal.bytes < need || (int64_t)op->kk2.bytes < (int64_t)k * k * 8)
+ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* d_status) {
+  // Householder + QL in FP32 (fast pipes), then two Ogita-Aishima refinement
+  // steps in FP64 (k x k GEMMs over all SMs) restore FP64 accuracy.
+  const int64_t kk = (int64_t)k * k;
+  const size_t need_f = (size_t)(2 * kk + 8 * (int64_t)k + 64) * sizeof(float);
+  if ((int64_t)op->scal.bytes < (kScalJacobi + k) * (int64_t)sizeof(double) ||
+      (int64_t)op->kk2.bytes < kk * 8 || op->kk3.bytes < need_f)
     return TTG_BAD_ARG;
-  double* cs = op->scal.as<double>() + kScalJacobi;
-  double* wtmp = cs + 4 * (k + 2);
-  k_symmetrize<<<64, 256, 0, op->stream>>>(A, k);
+  const size_t need_r = (size_t)(5 * kk + 8) * sizeof(double);
+  if (op->eigbuf.bytes < need_r) TTG_TRY(op->eigbuf.alloc(need_r));
+  cudaStream_t st = op->stream;
+  double* wtmp = op->scal.as<double>() + kScalJacobi;
+  double* Vd = op->kk2.as<double>();
+  double* Gm = op->eigbuf.as<double>();
+  double* AV = Gm + kk;
+  double* Sm = AV + kk;
+  double* E = Sm + kk;
+  double* VE = E + kk;
+  double* normA = VE + kk;
+  float* Af = op->kk3.as<float>();
+  float* Qf = Af + kk;
+  float* wf = Qf + kk;
+  k_symmetrize<<<64, 256, 0, st>>>(A, k);
   TTG_LAUNCHED(op);
-  k_jacobi<<<1, 1024, 0, op->stream>>>(A, op->kk2.as<double>(), wtmp, k, 60, 1e-14, d_status,
-                                       cs);
+  k_frob2<<<1, 1024, 0, st>>>(A, kk, normA);
   TTG_LAUNCHED(op);
-  k_sort_eig<<<(k + 127) / 128, 128, 0, op->stream>>>(wtmp, op->kk2.as<double>(), w, V, k);
+  // FP32 stage: Af <- A; tridiagonalise + QL (scratch: vectors + reflectors)
+  if (op->eigf.bytes < (size_t)(kk + 6 * (int64_t)k + 64) * sizeof(float))
+    TTG_TRY(op->eigf.alloc((size_t)(kk + 6 * (int64_t)k + 64) * sizeof(float)));
+  k_d2f_vec<<<64, 256, 0, st>>>(A, Af, kk);
   TTG_LAUNCHED(op);
+  k_tridiag_ql<float><<<1, 1024, 0, st>>>(Af, Qf, wf, k, d_status, op->eigf.as<float>());
+  TTG_LAUNCHED(op);
+  k_f2d_vec<<<64, 256, 0, st>>>(Qf, Vd, kk);
+  TTG_LAUNCHED(op);
+  const DOp Vt{Vd, (int64_t)k, 1, 0}, Vn{Vd, 1, (int64_t)k, 0}, An{A, 1, (int64_t)k, 0};
+  for (int it = 0; it <= 2; ++it) {
+    TTG_TRY(dgemm(st, k, k, k, 1, Vt, Vn, Gm, 1, k, 0, op->partial));           // G = V^T V
+    TTG_TRY(dgemm(st, k, k, k, 1, An, Vn, AV, 1, k, 0, op->partial));           // A V
+    TTG_TRY(dgemm(st, k, k, k, 1, Vt, DOp{AV, 1, (int64_t)k, 0}, Sm, 1, k, 0,
+                  op->partial));                                                // S = V^T A V
+    op->launches += 6;
+    k_oa_step<<<1, 1024, 0, st>>>(Gm, Sm, k, normA, E, wtmp);
+    TTG_LAUNCHED(op);
+    if (it == 2) break;                                                        // final lam only
+    TTG_TRY(dgemm(st, k, k, k, 1, Vn, DOp{E, 1, (int64_t)k, 0}, VE, 1, k, 0, op->partial));
+    op->launches += 2;
+    k_add<<<64, 256, 0, st>>>(Vd, VE, kk);
+    TTG_LAUNCHED(op);
+  }
+  k_sort_eig<<<(k + 127) / 128, 128, 0, st>>>(wtmp, Vd, w, V, k);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+// Largest r eigenpairs (descending) of a symmetric n x n column-major A, FP64:
+// Householder tridiagonalisation, bisection + inverse iteration on T, back-
+// transform U = Q Z.  w (r), U (n x r column-major) on the device; also the
+// trace of A into *trace_dev.
+ttg_status sym_topk(ttg_op* op, double* A, int n, int r, double* w, double* U, int* d_status) {
+  if (r < 1 || r > n) return TTG_BAD_ARG;
+  const int64_t nn = (int64_t)n * n;
+  const size_t need = (size_t)(2 * nn + 6 * (int64_t)n + 64 + (int64_t)r * (4 * n + n)) * sizeof(double);
+  if (op->eigbuf.bytes < need) TTG_TRY(op->eigbuf.alloc(need));
+  cudaStream_t st = op->stream;
+  double* Q = op->eigbuf.as<double>();
+  double* scratch = Q + nn;                         // v p d e | reflectors (n*n) | rot
+  double* Zt = scratch + nn + 6 * (int64_t)n + 64;  // r x n (tridiagonal basis)
+  double* work = Zt + (int64_t)r * n;               // r x 4n
+  k_symmetrize<<<64, 256, 0, st>>>(A, n);
+  TTG_LAUNCHED(op);
+  k_tridiag_ql<double, false><<<1, 1024, 0, st>>>(A, Q, w, n, d_status, scratch);
+  TTG_LAUNCHED(op);
+  const double* d = scratch + 2 * n;
+  const double* e = scratch + 3 * n;
+  k_tridiag_topk<<<1, 256, 0, st>>>(d, e, n, r, w, Zt, work);
+  TTG_LAUNCHED(op);
+  // U = Q Zt  (n x n)(n x r)
+  TTG_TRY(dgemm(st, n, r, n, 1, DOp{Q, 1, (int64_t)n, 0}, DOp{Zt, 1, (int64_t)n, 0}, U, 1, n, 0,
+                op->partial));
+  op->launches += 2;
   return TTG_OK;
 }
 

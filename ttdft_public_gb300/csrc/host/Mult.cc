@@ -28,12 +28,14 @@ void AX::setup_system(ProjectHamiltonianSparse& H) {
   Mat A = H.H_loc;
   if (!A || A->kind != _p_Mat::AIJ || A->m != A->n) throw std::invalid_argument("H_loc: square AIJ");
   const int32_t nproj = H.C ? (int32_t)H.C->m : 0;
-  ttdft::check(ttg_op_create(A->m, A->row_ptr.data(), A->col.data(), A->val.data(), nproj,
-                             nproj ? H.C->row_ptr.data() : nullptr,
-                             nproj ? H.C->col.data() : nullptr,
-                             nproj ? H.C->val.data() : nullptr, nproj ? H.D.data() : nullptr,
-                             num_wfns_, &op_),
-               "ttg_op_create");
+  const bool tucker = H.tucker_ranks[0] > 0;
+  ttdft::check(ttg_op_create_tucker(A->m, A->row_ptr.data(), A->col.data(), A->val.data(), nproj,
+                                    nproj ? H.C->row_ptr.data() : nullptr,
+                                    nproj ? H.C->col.data() : nullptr,
+                                    nproj ? H.C->val.data() : nullptr,
+                                    nproj ? H.D.data() : nullptr,
+                                    tucker ? H.tucker_ranks : nullptr, num_wfns_, &op_),
+               "ttg_op_create_tucker");
   ttdft::set_current_op(op_);
 }
 

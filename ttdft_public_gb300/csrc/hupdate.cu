@@ -1,0 +1,210 @@
+// New values of H_loc for a new effective potential, on the device.
+//
+// The reference rebuilds H_loc on the host every SCF iteration
+// (ProjectHamiltonianSparse::Create_Hloc, dft/ProjectHamiltonianSparse.cc:
+// 330-575, called from main.cc:965-972): for row I = (xI, yI, zI) and column
+// J = (xJ, yJ, zJ)
+//   H[I,J] = 0.5 (DX MY MZ + MX DY MZ + MX MY DZ)[I,J]
+//          + sum_abc G_abc PX_a[xI,xJ] PY_b[yI,yJ] PZ_c[zI,zJ]
+// with V_eff = sum_abc G_abc u_a(x) v_b(y) w_c(z) its Tucker decomposition
+// (main.cc:951-955) and PX_a[i,j] = int psi_i u_a psi_j.
+//
+// Here the sparsity pattern is the one fixed when the operator was created,
+// and the values are recomputed in place: the Tucker sum is factorised
+// through (x-pair, y-pair) intermediates
+//   T1[xp][b][c]     = sum_a PX_a[xp] G_abc                  (one FP64 GEMM)
+//   T2[yp][xp][c]    = sum_b PY_b[yp] T1[xp][b][c]           (batched FP64 GEMM)
+//   H_pot[I,J]       = sum_c PZ_c[zp] T2[yp][xp][c]          (per entry, r_c FMAs)
+// and each new value is written straight into every device format through
+// the position maps recorded when the formats were packed.  FP64 throughout.
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ttg_internal.cuh"
+
+namespace ttg {
+namespace {
+
+struct UpdateArgs {
+  const int64_t* row_ptr;
+  const int* col;
+  const int* rg_pos;
+  const int* tile_base;
+  const uint8_t* tile_slot;
+  int rx, ry, rz;
+  int bw[3];                  // half-bandwidths of the pair tables
+  const double* kin;          // DX DY DZ MX MY MZ, each r_d x r_d row-major
+  const double* T2;           // [yp][xp][c]
+  const double* PZp;          // [zp][c]
+  int rc;                     // Tucker rank of the potential along z
+  int64_t nxp;
+  double* v64;
+  float2* vdf;
+  float* v32;
+  __nv_bfloat16* v16;
+  float* t32;
+  __nv_bfloat16* t16;
+  int64_t n;
+};
+
+__device__ __forceinline__ int pair_index(int i, int j, int bw) {
+  const int d = j - i;
+  return (d < -bw || d > bw) ? -1 : i * (2 * bw + 1) + d + bw;
+}
+
+__global__ void k_update_values(UpdateArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= a.n) return;
+  const int xI = (int)(row % a.rx);
+  const int yI = (int)((row / a.rx) % a.ry);
+  const int zI = (int)(row / ((int64_t)a.rx * a.ry));
+  const int rx = a.rx, ry = a.ry, rz = a.rz;
+  const double* DX = a.kin;
+  const double* DY = DX + rx * rx;
+  const double* DZ = DY + ry * ry;
+  const double* MX = DZ + rz * rz;
+  const double* MY = MX + rx * rx;
+  const double* MZ = MY + ry * ry;
+  for (int64_t e = a.row_ptr[row] + lane; e < a.row_ptr[row + 1]; e += 32) {
+    const int J = a.col[e];
+    const int xJ = J % rx, yJ = (J / rx) % ry, zJ = J / (rx * ry);
+    const double dx = DX[xI * rx + xJ], mx = MX[xI * rx + xJ];
+    const double dy = DY[yI * ry + yJ], my = MY[yI * ry + yJ];
+    const double dz = DZ[zI * rz + zJ], mz = MZ[zI * rz + zJ];
+    double val = 0.5 * (dx * my * mz + mx * dy * mz + mx * my * dz);
+    const int xp = pair_index(xI, xJ, a.bw[0]);
+    const int yp = pair_index(yI, yJ, a.bw[1]);
+    const int zp = pair_index(zI, zJ, a.bw[2]);
+    if (xp >= 0 && yp >= 0 && zp >= 0) {
+      const double* t2 = a.T2 + ((int64_t)yp * a.nxp + xp) * a.rc;
+      const double* pz = a.PZp + (int64_t)zp * a.rc;
+      double s = 0.0;
+      for (int c = 0; c < a.rc; ++c) s = fma(pz[c], t2[c], s);
+      val += s;
+    }
+    const int p = a.rg_pos[e];
+    a.v64[p] = val;
+    if (a.vdf) {
+      const float h = __double2float_rn(val);
+      a.vdf[p] = make_float2(h, __double2float_rn(val - (double)h));
+    }
+    if (a.v32) a.v32[p] = (float)val;
+    if (a.v16) a.v16[p] = __double2bfloat16(val);
+    if (a.t32) {
+      // fragment order of spmm_tc.cu: TF32 lane 4g+(j%4), element j/4;
+      // BF16 lane 4g+((j%8)/2), element (j%2) + 2*(j/8)
+      const int base = a.tile_base[e];
+      const int j = a.tile_slot[e];
+      a.t32[(int64_t)(base + (j & 3)) * 4 + (j >> 2)] = (float)val;
+      a.t16[(int64_t)(base + ((j & 7) >> 1)) * 4 + (j & 1) + 2 * (j >> 3)] = __double2bfloat16(val);
+    }
+  }
+}
+
+}  // namespace
+}  // namespace ttg
+
+using namespace ttg;
+
+extern "C" {
+
+ttg_status ttg_op_set_kinetic(ttg_op* op, const double* dx, const double* dy, const double* dz,
+                              const double* mx, const double* my, const double* mz) {
+  if (!op || !op->keep_pattern || !dx || !dy || !dz || !mx || !my || !mz) return TTG_BAD_ARG;
+  Pattern& P = op->pattern;
+  const int rx = P.r[0], ry = P.r[1], rz = P.r[2];
+  const size_t cnt = 2 * ((size_t)rx * rx + (size_t)ry * ry + (size_t)rz * rz);
+  if (!P.kin.p) TTG_TRY(P.kin.alloc(cnt * 8));
+  std::vector<double> h;
+  h.reserve(cnt);
+  h.insert(h.end(), dx, dx + rx * rx);
+  h.insert(h.end(), dy, dy + ry * ry);
+  h.insert(h.end(), dz, dz + rz * rz);
+  h.insert(h.end(), mx, mx + rx * rx);
+  h.insert(h.end(), my, my + ry * ry);
+  h.insert(h.end(), mz, mz + rz * rz);
+  TTG_CUDA_TRY(cudaMemcpyAsync(P.kin.p, h.data(), cnt * 8, cudaMemcpyHostToDevice, op->stream));
+  TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
+  P.kinetic_set = true;
+  return TTG_OK;
+}
+
+ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const double* G,
+                                   const double* px, const double* py, const double* pz) {
+  if (!op || !op->keep_pattern || !op->pattern.kinetic_set || !pot_ranks || !G || !px || !py ||
+      !pz)
+    return TTG_BAD_ARG;
+  Pattern& P = op->pattern;
+  const int rx = P.r[0], ry = P.r[1], rz = P.r[2];
+  const int ra = pot_ranks[0], rb = pot_ranks[1], rc = pot_ranks[2];
+  if (ra <= 0 || rb <= 0 || rc <= 0) return TTG_BAD_ARG;
+  const int bw[3] = {P.bw[0], P.bw[1], P.bw[2]};
+  const int64_t nxp = (int64_t)rx * (2 * bw[0] + 1);
+  const int64_t nyp = (int64_t)ry * (2 * bw[1] + 1);
+  const int64_t nzp = (int64_t)rz * (2 * bw[2] + 1);
+  // pair tables PXp[xp][a] = PX_a[i][j] (host: O(pairs * rank))
+  auto pairs = [](const double* pm, int r, int rk, int b, std::vector<double>& out) {
+    const int64_t np = (int64_t)r * (2 * b + 1);
+    out.assign(np * rk, 0.0);
+    for (int i = 0; i < r; ++i)
+      for (int d = -b; d <= b; ++d) {
+        const int j = i + d;
+        if (j < 0 || j >= r) continue;
+        const int64_t p = (int64_t)i * (2 * b + 1) + d + b;
+        for (int a = 0; a < rk; ++a) out[p * rk + a] = pm[((int64_t)a * r + i) * r + j];
+      }
+  };
+  std::vector<double> hx, hy, hz;
+  pairs(px, rx, ra, bw[0], hx);
+  pairs(py, ry, rb, bw[1], hy);
+  pairs(pz, rz, rc, bw[2], hz);
+  const int64_t ncore = (int64_t)ra * rb * rc;
+  const int64_t off_x = 0, off_y = off_x + nxp * ra, off_z = off_y + nyp * rb;
+  const int64_t off_g = off_z + nzp * rc, off_t1 = off_g + ncore;
+  const int64_t off_t2 = off_t1 + nxp * rb * rc, total = off_t2 + nyp * nxp * rc;
+  if ((int64_t)P.work.bytes < total * 8) TTG_TRY(P.work.alloc(total * 8));
+  double* w = P.work.as<double>();
+  cudaStream_t st = op->stream;
+  TTG_CUDA_TRY(cudaMemcpyAsync(w + off_x, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice, st));
+  TTG_CUDA_TRY(cudaMemcpyAsync(w + off_y, hy.data(), hy.size() * 8, cudaMemcpyHostToDevice, st));
+  TTG_CUDA_TRY(cudaMemcpyAsync(w + off_z, hz.data(), hz.size() * 8, cudaMemcpyHostToDevice, st));
+  TTG_CUDA_TRY(cudaMemcpyAsync(w + off_g, G, ncore * 8, cudaMemcpyHostToDevice, st));
+  // T1[xp][(b,c)] = sum_a PXp[xp][a] G[a + ra (b + rb c)]
+  TTG_TRY(dgemm(st, (int)nxp, rb * rc, ra, 1, DOp{w + off_x, ra, 1, 0}, DOp{w + off_g, 1, ra, 0},
+                w + off_t1, (int64_t)rb * rc, 1, 0, P.work2));
+  // T2[yp][xp][c] = sum_b PYp[yp][b] T1[xp][b + rb c]   (batch over xp)
+  TTG_TRY(dgemm(st, (int)nyp, rc, rb, (int)nxp, DOp{w + off_y, rb, 1, 0},
+                DOp{w + off_t1, 1, rb, (int64_t)rb * rc}, w + off_t2, nxp * rc, 1, rc, P.work2));
+  UpdateArgs a{};
+  a.row_ptr = P.row_ptr.as<int64_t>();
+  a.col = P.col.as<int>();
+  a.rg_pos = P.rg_pos.as<int>();
+  a.tile_base = P.tile_base.as<int>();
+  a.tile_slot = P.tile_slot.as<uint8_t>();
+  a.rx = rx;
+  a.ry = ry;
+  a.rz = rz;
+  for (int d = 0; d < 3; ++d) a.bw[d] = bw[d];
+  a.kin = P.kin.as<double>();
+  a.T2 = w + off_t2;
+  a.PZp = w + off_z;
+  a.rc = rc;
+  a.nxp = nxp;
+  a.v64 = op->rg.v64.as<double>();
+  a.vdf = op->rg.vdf.as<float2>();
+  a.v32 = op->rg.v32.as<float>();
+  a.v16 = op->rg.v16.as<__nv_bfloat16>();
+  a.t32 = op->tiles.n_tiles > 0 && P.tile_base.p ? op->tiles.v32.as<float>() : nullptr;
+  a.t16 = op->tiles.v16.as<__nv_bfloat16>();
+  a.n = op->n;
+  const int wpb = 8;
+  k_update_values<<<(unsigned)((op->n + wpb - 1) / wpb), 32 * wpb, 0, st>>>(a);
+  TTG_LAUNCHED(op);
+  TTG_CUDA_TRY(cudaStreamSynchronize(st));
+  return TTG_OK;
+}
+
+}  // extern "C"

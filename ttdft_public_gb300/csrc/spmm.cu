@@ -232,6 +232,105 @@ __global__ void __launch_bounds__(512) k_cheb_step(
   }
 }
 
+// Y = H X with FP64 values carried as unevaluated pairs of FP32 (hi + lo,
+// ~44 significant bits), on the FP32 pipes.  Each product uses the exact
+// FMA residual (a_hi*b_hi = p + fma(a_hi, b_hi, -p)) plus the two cross terms,
+// and is accumulated with Knuth's error-free two-sum into (hi, lo).  GB300
+// runs FP32 at many times its FP64 rate, so this carries the Rayleigh-Ritz
+// product H X at FP64-level accuracy several times faster than FP64 FMAs.
+// Source rows are float2 (hi, lo) pairs; H slots are float2 pairs too.
+template <int G>
+__global__ void __launch_bounds__(512) k_apply_df64(
+    const int64_t* __restrict__ gptr, const int* __restrict__ gcol,
+    const float2* __restrict__ gval, const float2* __restrict__ src, double* __restrict__ dst,
+    int64_t n, int k, int64_t ld) {
+  constexpr int CH = 32;
+  __shared__ __align__(16) int s_col[2][CH];
+  __shared__ __align__(16) float2 s_val[2][CH * G];
+  const int64_t g = blockIdx.x;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int c0 = blockIdx.y * blockDim.x + tid;       // state (column) of this thread
+  const bool active = c0 < k;
+  const int64_t s0 = gptr[g], s1 = gptr[g + 1];
+  const int nchunks = (int)((s1 - s0 + CH - 1) / CH);
+  auto stage = [&](int c, int buf) {
+    const int64_t base = s0 + (int64_t)c * CH;
+    const int cnt = (int)(s1 - base < CH ? s1 - base : CH);   // multiple of 4
+    const int ncol16 = cnt / 4;
+    const int nval16 = cnt * G * 8 / 16;
+    const char* gc = reinterpret_cast<const char*>(gcol + base);
+    const char* gv = reinterpret_cast<const char*>(gval + base * G);
+    char* sc = reinterpret_cast<char*>(s_col[buf]);
+    char* sv = reinterpret_cast<char*>(s_val[buf]);
+    for (int i = tid; i < ncol16 + nval16; i += nthr) {
+      if (i < ncol16) cp_async16(sc + 16 * i, gc + 16 * i);
+      else cp_async16(sv + 16 * (i - ncol16), gv + 16 * (i - ncol16));
+    }
+  };
+  float hi[G], lo[G];
+#pragma unroll
+  for (int r = 0; r < G; ++r) hi[r] = lo[r] = 0.f;
+  if (nchunks > 0) stage(0, 0);
+  cp_async_commit();
+  for (int c = 0; c < nchunks; ++c) {
+    const int buf = c & 1;
+    if (c + 1 < nchunks) stage(c + 1, buf ^ 1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const int cnt = (int)(s1 - (s0 + (int64_t)c * CH) < CH ? s1 - (s0 + (int64_t)c * CH) : CH);
+    if (active) {
+#pragma unroll 2
+      for (int j = 0; j < cnt; ++j) {
+        const float2 x = __ldg(src + (int64_t)s_col[buf][j] * ld + c0);
+        const float2* hv = &s_val[buf][j * G];
+#pragma unroll
+        for (int r = 0; r < G; ++r) {
+          const float2 h = hv[r];
+          const float p = h.x * x.x;
+          float e = fmaf(h.x, x.x, -p);
+          e = fmaf(h.x, x.y, e);
+          e = fmaf(h.y, x.x, e);
+          const float s = hi[r] + p;
+          const float bb = s - hi[r];
+          const float err = (hi[r] - (s - bb)) + (p - bb);
+          hi[r] = s;
+          lo[r] += err + e;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (!active) return;
+#pragma unroll
+  for (int r = 0; r < G; ++r) {
+    const int64_t row = g * G + r;
+    if (row < n) dst[row * ld + c0] = (double)hi[r] + (double)lo[r];
+  }
+}
+
+__global__ void k_split_df64(const double* __restrict__ src, float2* __restrict__ dst,
+                             int64_t rows, int k, int64_t ld) {
+  const int64_t total = rows * (int64_t)k;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / k;
+    const int c = (int)(i - r * k);
+    const double v = src[r * ld + c];
+    const float h = __double2float_rn(v);
+    dst[r * ld + c] = make_float2(h, __double2float_rn(v - (double)h));
+  }
+}
+
+__global__ void k_split_vals(const double* __restrict__ src, float2* __restrict__ dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = src[i];
+    const float h = __double2float_rn(v);
+    dst[i] = make_float2(h, __double2float_rn(v - (double)h));
+  }
+}
+
 // k == 1 (Lanczos SpMV): one warp per row group, lanes split the slots.
 template <int G>
 __global__ void k_spmv_rg(const int64_t* __restrict__ gptr, const int* __restrict__ gcol,
@@ -263,31 +362,39 @@ __global__ void k_spmv_rg(const int64_t* __restrict__ gptr, const int* __restric
   }
 }
 
-// W[a,:] = sum_J Cd[a,J] Y[J,:] (Cd = diag(D) C), written to row n + a.
-// blockDim = (bx columns, by slices); grid = (nproj, ceil(k / bx)).
+// W[a,:] = sum_J Cd[a,J] Y[J,:] (Cd = diag(D) C), written to row n + a of the
+// source block.  Two launches so that all SMs take part: (1) grid (nproj,
+// splits): each CTA sums kProjChunk entries of one projector row into a
+// partial row; (2) the partial rows are summed in a fixed order (bitwise
+// reproducible) and stored.
+constexpr int kProjChunk = 128;
+
 template <typename TS, typename TA>
-__global__ void k_proj_w(const int64_t* __restrict__ cptr, const int* __restrict__ ccol,
-                         const double* __restrict__ cval, TS* src, int64_t n, int k,
-                         int64_t ld) {
-  extern __shared__ unsigned char smem_raw[];
-  TA* red = reinterpret_cast<TA*>(smem_raw);
-  const int a = blockIdx.x;
-  const int c = blockIdx.y * blockDim.x + threadIdx.x;
-  TA acc = TA(0);
-  if (c < k) {
-    for (int64_t e = cptr[a] + threadIdx.y; e < cptr[a + 1]; e += blockDim.y) {
-      const TA h = (TA)cval[e];
+__global__ void k_proj_partial(const int64_t* __restrict__ cptr, const int* __restrict__ ccol,
+                               const double* __restrict__ cval, const TS* __restrict__ src, int k,
+                               int64_t ld, TA* __restrict__ part, int nsplit) {
+  const int a = blockIdx.x, sp = blockIdx.y;
+  const int64_t e0 = cptr[a] + (int64_t)sp * kProjChunk;
+  const int64_t e1 = min(cptr[a + 1], e0 + kProjChunk);
+  for (int c = threadIdx.x; c < k; c += blockDim.x) {
+    TA acc = TA(0);
+    for (int64_t e = e0; e < e1; ++e) {
       TA x;
       if constexpr (sizeof(TS) == sizeof(TA)) x = src[(int64_t)ccol[e] * ld + c];
       else x = to_acc<TS>(src[(int64_t)ccol[e] * ld + c]);
-      acc = fma(h, x, acc);
+      acc = fma((TA)cval[e], x, acc);
     }
+    part[((int64_t)a * nsplit + sp) * k + c] = acc;
   }
-  red[threadIdx.y * blockDim.x + threadIdx.x] = acc;
-  __syncthreads();
-  if (threadIdx.y == 0 && c < k) {
+}
+
+template <typename TS, typename TA>
+__global__ void k_proj_reduce(const TA* __restrict__ part, int nsplit, TS* src, int64_t n, int k,
+                              int64_t ld) {
+  const int a = blockIdx.x;
+  for (int c = threadIdx.x; c < k; c += blockDim.x) {
     TA s = TA(0);
-    for (int y = 0; y < (int)blockDim.y; ++y) s += red[y * blockDim.x + threadIdx.x];
+    for (int sp = 0; sp < nsplit; ++sp) s += part[((int64_t)a * nsplit + sp) * k + c];
     if constexpr (sizeof(TS) == sizeof(TA)) src[(n + a) * ld + c] = s;
     else src[(n + a) * ld + c] = __float2bfloat16_rn((float)s);
   }
@@ -429,6 +536,8 @@ ttg_status build_row_groups(ttg_op* op, int64_t n, const int64_t* hp, const int3
   const int64_t slots = gptr[ng];
   std::vector<int32_t> gcol(slots);
   std::vector<double> gval(slots * G, 0.0);
+  // position of every H_loc entry in the value array (for value updates)
+  std::vector<int32_t> rgpos(op->keep_pattern ? hp[n] : 0);
 #pragma omp parallel
   {
     std::vector<int32_t> cols;
@@ -446,6 +555,7 @@ ttg_status build_row_groups(ttg_op* op, int64_t n, const int64_t* hp, const int3
         for (int64_t e = hp[r]; e < hp[r + 1]; ++e) {
           while (cols[s] != hc[e]) ++s;
           gval[(base + s) * G + (r - r0)] = hv[e];
+          if (!rgpos.empty()) rgpos[e] = (int32_t)((base + s) * G + (r - r0));
         }
         if (nproj > 0)
           for (int64_t e = tp[r]; e < tp[r + 1]; ++e) {
@@ -461,8 +571,7 @@ ttg_status build_row_groups(ttg_op* op, int64_t n, const int64_t* hp, const int3
   TTG_TRY(rg.gptr.alloc((ng + 1) * sizeof(int64_t)));
   TTG_TRY(rg.gcol.alloc(std::max<int64_t>(slots, 4) * sizeof(int32_t)));
   TTG_TRY(rg.v64.alloc(std::max<int64_t>(slots, 4) * G * sizeof(double)));
-  TTG_TRY(rg.v32.alloc(std::max<int64_t>(slots, 4) * G * sizeof(float)));
-  TTG_TRY(rg.v16.alloc(std::max<int64_t>(slots, 4) * G * sizeof(__nv_bfloat16)));
+
   TTG_CUDA_TRY(cudaMemcpyAsync(rg.gptr.p, gptr.data(), (ng + 1) * sizeof(int64_t),
                                cudaMemcpyHostToDevice, op->stream));
   if (slots > 0) {
@@ -470,18 +579,15 @@ ttg_status build_row_groups(ttg_op* op, int64_t n, const int64_t* hp, const int3
                                  cudaMemcpyHostToDevice, op->stream));
     TTG_CUDA_TRY(cudaMemcpyAsync(rg.v64.p, gval.data(), slots * G * sizeof(double),
                                  cudaMemcpyHostToDevice, op->stream));
-    k_convert_vals<float><<<grid_for(slots * G, 256), 256, 0, op->stream>>>(
-        rg.v64.as<double>(), rg.v32.as<float>(), slots * G);
-    TTG_LAUNCHED(op);
-    k_convert_vals<__nv_bfloat16><<<grid_for(slots * G, 256), 256, 0, op->stream>>>(
-        rg.v64.as<double>(), rg.v16.as<__nv_bfloat16>(), slots * G);
-    TTG_LAUNCHED(op);
+
   }
   // C with D folded in (C_nloc = diag(D) C), plus an FP32 copy
   Csr& C = op->C;
   C.rows = nproj;
   C.cols = n;
   C.nnz = nproj > 0 ? cp[nproj] : 0;
+  C.max_row_nnz = 0;
+  for (int a = 0; a < nproj; ++a) C.max_row_nnz = std::max<int64_t>(C.max_row_nnz, cp[a + 1] - cp[a]);
   if (nproj > 0) {
     TTG_TRY(C.ptr.alloc((nproj + 1) * sizeof(int64_t)));
     TTG_TRY(C.col.alloc(std::max<int64_t>(C.nnz, 1) * sizeof(int32_t)));
@@ -500,10 +606,69 @@ ttg_status build_row_groups(ttg_op* op, int64_t n, const int64_t* hp, const int3
   }
   op->nnz_h = hp[n];
   op->nnz_c = C.nnz;
+  if (op->keep_pattern && hp[n] > 0) {
+    if (slots * G >= INT32_MAX) return TTG_BAD_ARG;
+    Pattern& P = op->pattern;
+    // half-bandwidth of the pattern in each Tucker direction
+    const int rx = P.r[0], ry = P.r[1];
+    int bx = 0, by = 0, bz = 0;
+#pragma omp parallel for reduction(max : bx, by, bz) schedule(static)
+    for (int64_t I = 0; I < n; ++I) {
+      const int xI = (int)(I % rx), yI = (int)((I / rx) % ry), zI = (int)(I / ((int64_t)rx * ry));
+      for (int64_t e = hp[I]; e < hp[I + 1]; ++e) {
+        const int J = hc[e];
+        bx = std::max(bx, std::abs(J % rx - xI));
+        by = std::max(by, std::abs((J / rx) % ry - yI));
+        bz = std::max(bz, std::abs(J / (rx * ry) - zI));
+      }
+    }
+    P.bw[0] = bx;
+    P.bw[1] = by;
+    P.bw[2] = bz;
+    TTG_TRY(P.row_ptr.alloc((n + 1) * sizeof(int64_t)));
+    TTG_TRY(P.col.alloc(hp[n] * sizeof(int32_t)));
+    TTG_TRY(P.rg_pos.alloc(hp[n] * sizeof(int32_t)));
+    TTG_CUDA_TRY(cudaMemcpyAsync(P.row_ptr.p, hp, (n + 1) * sizeof(int64_t),
+                                 cudaMemcpyHostToDevice, op->stream));
+    TTG_CUDA_TRY(cudaMemcpyAsync(P.col.p, hc, hp[n] * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                 op->stream));
+    TTG_CUDA_TRY(cudaMemcpyAsync(P.rg_pos.p, rgpos.data(), hp[n] * sizeof(int32_t),
+                                 cudaMemcpyHostToDevice, op->stream));
+    op->device_bytes += P.row_ptr.bytes + P.col.bytes + P.rg_pos.bytes;
+  }
   // host vectors above are freed on return: wait for the copies
   TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
-  op->device_bytes += rg.gptr.bytes + rg.gcol.bytes + rg.v64.bytes + rg.v32.bytes +
-                      rg.v16.bytes + C.ptr.bytes + C.col.bytes + C.val.bytes;
+  op->device_bytes += rg.gptr.bytes + rg.gcol.bytes + rg.v64.bytes + C.ptr.bytes + C.col.bytes +
+                      C.val.bytes;
+  return TTG_OK;
+}
+
+// FP32 / BF16 / (hi, lo) copies of the row-group values, made from the FP64
+// values on first use (the tensor-core format serves the FP32 and BF16
+// degrees, so these are needed only for block widths it does not take).
+static ttg_status rg_values(ttg_op* op, int prec, void** out) {
+  RowGroups& rg = op->rg;
+  const int64_t cnt = std::max<int64_t>(rg.slots, 4) * kGroupRows;
+  const int grid = grid_for(cnt, 256);
+  if (prec == TTG_PREC_FP32 && !rg.v32.p) {
+    TTG_TRY(rg.v32.alloc(cnt * sizeof(float)));
+    k_convert_vals<float><<<grid, 256, 0, op->stream>>>(rg.v64.as<double>(), rg.v32.as<float>(), cnt);
+    TTG_LAUNCHED(op);
+    op->device_bytes += rg.v32.bytes;
+  } else if (prec == TTG_PREC_BF16 && !rg.v16.p) {
+    TTG_TRY(rg.v16.alloc(cnt * sizeof(__nv_bfloat16)));
+    k_convert_vals<__nv_bfloat16><<<grid, 256, 0, op->stream>>>(rg.v64.as<double>(),
+                                                               rg.v16.as<__nv_bfloat16>(), cnt);
+    TTG_LAUNCHED(op);
+    op->device_bytes += rg.v16.bytes;
+  } else if (prec == TTG_PREC_DF64 && !rg.vdf.p) {
+    TTG_TRY(rg.vdf.alloc(cnt * sizeof(float2)));
+    k_split_vals<<<grid, 256, 0, op->stream>>>(rg.v64.as<double>(), rg.vdf.as<float2>(), cnt);
+    TTG_LAUNCHED(op);
+    op->device_bytes += rg.vdf.bytes;
+  }
+  *out = prec == TTG_PREC_FP32 ? rg.v32.p : prec == TTG_PREC_BF16 ? rg.v16.p
+         : prec == TTG_PREC_DF64 ? rg.vdf.p : rg.v64.p;
   return TTG_OK;
 }
 
@@ -527,6 +692,8 @@ static ttg_status launch_step_t(ttg_op* op, const TV* vals, const void* src, con
 ttg_status launch_cheb_step(ttg_op* op, int prec, const void* src, const void* xold, void* dst,
                             int k, double alpha, double beta, double delta) {
   if (k <= 0 || k > op->max_k) return TTG_BAD_ARG;
+  if (tc_supported(op, prec, k))
+    return launch_cheb_tc(op, prec, src, xold, dst, k, alpha, beta, delta);
   if (prec == TTG_PREC_FP64) {
     if (k == 1) {
       const int wpb = 8;
@@ -544,6 +711,10 @@ ttg_status launch_cheb_step(ttg_op* op, int prec, const void* src, const void* x
                                                       dst, k, alpha, beta, delta);
     return launch_step_t<double, double, double, 1>(op, op->rg.v64.as<double>(), src, xold, dst,
                                                     k, alpha, beta, delta);
+  }
+  if (prec == TTG_PREC_FP32 || prec == TTG_PREC_BF16) {
+    void* vp = nullptr;
+    TTG_TRY(rg_values(op, prec, &vp));
   }
   if (prec == TTG_PREC_FP32) {
     if (k % 4 == 0 && k > 256)
@@ -567,27 +738,54 @@ ttg_status launch_cheb_step(ttg_op* op, int prec, const void* src, const void* x
   return TTG_BAD_ARG;
 }
 
-ttg_status launch_proj_w(ttg_op* op, int prec, void* src, int k) {
-  if (op->nproj == 0) return TTG_OK;
-  const int bx = std::min(((k + 31) / 32) * 32, 256);
-  const int by = std::max(1, 512 / bx);
-  dim3 grid(op->nproj, (k + bx - 1) / bx);
-  dim3 block(bx, by);
-  if (prec == TTG_PREC_FP64) {
-    k_proj_w<double, double><<<grid, block, bx * by * sizeof(double), op->stream>>>(
-        op->C.ptr.as<int64_t>(), op->C.col.as<int>(), op->C.val.as<double>(),
-        reinterpret_cast<double*>(src), op->n, k, op->ld);
-  } else if (prec == TTG_PREC_FP32) {
-    k_proj_w<float, float><<<grid, block, bx * by * sizeof(float), op->stream>>>(
-        op->C.ptr.as<int64_t>(), op->C.col.as<int>(), op->C.val.as<double>(),
-        reinterpret_cast<float*>(src), op->n, k, op->ld);
-  } else {
-    k_proj_w<__nv_bfloat16, float><<<grid, block, bx * by * sizeof(float), op->stream>>>(
-        op->C.ptr.as<int64_t>(), op->C.col.as<int>(), op->C.val.as<double>(),
-        reinterpret_cast<__nv_bfloat16*>(src), op->n, k, op->ld);
+ttg_status launch_apply_df64(ttg_op* op, const double* src, double* dst, int k) {
+  if (k <= 0 || k > op->max_k) return TTG_BAD_ARG;
+  const size_t need = (size_t)(op->n + op->nproj) * op->ld * sizeof(float2);
+  if (op->wdf.bytes < need) {
+    TTG_TRY(op->wdf.alloc(need));
+    op->device_bytes += need;
   }
+  void* vdf = nullptr;
+  TTG_TRY(rg_values(op, TTG_PREC_DF64, &vdf));
+  const int64_t rows = op->n + op->nproj;
+  k_split_df64<<<grid_for(rows * k, 256), 256, 0, op->stream>>>(src, op->wdf.as<float2>(), rows,
+                                                                k, op->ld);
+  TTG_LAUNCHED(op);
+  if (op->rg.n_groups == 0) return TTG_OK;
+  const int threads = std::min(512, (k + 31) / 32 * 32);
+  dim3 grid((unsigned)op->rg.n_groups, (unsigned)((k + threads - 1) / threads));
+  k_apply_df64<kGroupRows><<<grid, threads, 0, op->stream>>>(
+      op->rg.gptr.as<int64_t>(), op->rg.gcol.as<int>(), op->rg.vdf.as<float2>(),
+      op->wdf.as<float2>(), dst, op->n, k, op->ld);
   TTG_LAUNCHED(op);
   return TTG_OK;
+}
+
+template <typename TS, typename TA>
+static ttg_status proj_w_t(ttg_op* op, TS* src, int k) {
+  const int nsplit = (int)((op->C.max_row_nnz + kProjChunk - 1) / kProjChunk);
+  if (nsplit == 0) return TTG_OK;
+  const size_t need = (size_t)op->nproj * nsplit * k * sizeof(TA);
+  if (op->wpart.bytes < need) {
+    TTG_TRY(op->wpart.alloc(need));
+    op->device_bytes += need;
+  }
+  const int threads = std::min(256, (k + 31) / 32 * 32);
+  k_proj_partial<TS, TA><<<dim3(op->nproj, nsplit), threads, 0, op->stream>>>(
+      op->C.ptr.as<int64_t>(), op->C.col.as<int>(), op->C.val.as<double>(), src, k, op->ld,
+      op->wpart.as<TA>(), nsplit);
+  TTG_LAUNCHED(op);
+  k_proj_reduce<TS, TA><<<op->nproj, threads, 0, op->stream>>>(op->wpart.as<TA>(), nsplit, src,
+                                                              op->n, k, op->ld);
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status launch_proj_w(ttg_op* op, int prec, void* src, int k) {
+  if (op->nproj == 0) return TTG_OK;
+  if (prec == TTG_PREC_FP64) return proj_w_t<double, double>(op, reinterpret_cast<double*>(src), k);
+  if (prec == TTG_PREC_FP32) return proj_w_t<float, float>(op, reinterpret_cast<float*>(src), k);
+  return proj_w_t<__nv_bfloat16, float>(op, reinterpret_cast<__nv_bfloat16*>(src), k);
 }
 
 ttg_status launch_convert(ttg_op* op, int from, int to, const void* src, void* dst, int64_t rows,

@@ -46,7 +46,7 @@ constexpr int kMaxLanczos = 512;    // Lanczos steps (T is at most this size)
 constexpr int64_t kScalLanczos = 0;      // alpha/beta pairs, 2*kMaxLanczos
 constexpr int64_t kScalFermi = 1024;     // mu, iterations, residual
 constexpr int64_t kScalEig = 2048;       // eigenvalues (k)
-constexpr int64_t kScalJacobi = 2048 + 4096;  // Jacobi rotation scratch
+constexpr int64_t kScalJacobi = 2048 + 4096;  // unsorted eigenvalues (k)
 
 // Device buffer owned by the library.
 struct DevBuf {
@@ -71,10 +71,41 @@ struct RowGroups {
   DevBuf v64;      // double [slots*G]
   DevBuf v32;      // float  [slots*G]
   DevBuf v16;      // bf16   [slots*G]
+  DevBuf vdf;      // float2 [slots*G]: FP64 values as (hi, lo) FP32 pairs
+};
+
+// 3-D row tiles of 64 rows for the tensor-core SpMM (spmm_tc.cu): per tile a
+// merged column list in chunks of 16 slots, H values pre-arranged in MMA
+// B-fragment order (FP32 for TF32, BF16), and the tile's original row ids.
+struct TileOp {
+  int64_t n_tiles = 0;
+  int64_t slots = 0;
+  DevBuf tptr;     // int64 [n_tiles+1], slot offsets (multiples of 16)
+  DevBuf tcol;     // int32 [slots]
+  DevBuf rowmap;   // int32 [n_tiles*64], -1 = padding
+  DevBuf v32;      // float, [chunk][8 n-tiles][32 lanes][4]
+  DevBuf v16;      // bf16,  [chunk][8 n-tiles][32 lanes][4]
+};
+
+// The fixed sparsity pattern of H_loc and where each entry lives in the device
+// formats, kept when the operator is created with Tucker ranks so that its
+// values can be recomputed on the device for a new potential (hupdate.cu).
+struct Pattern {
+  DevBuf row_ptr;    // int64 [n+1]
+  DevBuf col;        // int32 [nnz]
+  DevBuf rg_pos;     // int32 [nnz]: index into the row-group value arrays
+  DevBuf tile_base;  // int32 [nnz]: lane base of the entry's tile fragment
+  DevBuf tile_slot;  // uint8 [nnz]: slot of the entry within its 16-slot chunk
+  int32_t r[3] = {0, 0, 0};   // Tucker ranks of the basis
+  int32_t bw[3] = {0, 0, 0};  // max |coordinate difference| per direction over the entries
+  DevBuf kin;        // 6 r x r 1-D matrices: DX DY DZ MX MY MZ (row-major)
+  bool kinetic_set = false;
+  DevBuf work;       // pair tables and the Tucker intermediates
+  DevBuf work2;
 };
 
 struct Csr {
-  int64_t rows = 0, cols = 0, nnz = 0;
+  int64_t rows = 0, cols = 0, nnz = 0, max_row_nnz = 0;
   DevBuf ptr;      // int64
   DevBuf col;      // int32
   DevBuf val;      // double
@@ -91,13 +122,23 @@ struct ttg_op {
   int32_t max_k = 0;
   int64_t nnz_h = 0, nnz_c = 0;
   ttg::RowGroups rg;
+  ttg::TileOp tiles;          // tensor-core format (FP32/BF16 degrees)
+  bool tc_disabled = false;   // TTG_DISABLE_TC=1: CUDA-core kernels only
+  bool keep_pattern = false;  // Tucker ranks given: keep the pattern for value updates
+  ttg::Pattern pattern;
   ttg::Csr C;                 // C (nproj x n) with D folded in: C_nloc = diag(D) C
   // workspace (rows = n + nproj, row-major, ld = max_k padded)
   int64_t ld = 0;             // row stride in elements of the working blocks
   ttg::DevBuf w32a, w32b;     // FP32 working blocks
   ttg::DevBuf w16a, w16b;     // BF16 working blocks
   ttg::DevBuf w64;            // FP64 scratch block (n + nproj rows)
+  ttg::DevBuf wdf;            // float2 (hi, lo) copy of an FP64 block for the df64 SpMM
+  ttg::DevBuf wpart;          // projector partial sums (nproj x splits x k)
+  int rr_prec = TTG_PREC_DF64;  // arithmetic of the Rayleigh-Ritz product H X
   ttg::DevBuf kk0, kk1, kk2;  // k x k FP64 matrices
+  ttg::DevBuf kk3;            // eigensolver scratch (k*k + 6k doubles)
+  ttg::DevBuf eigbuf;         // eigensolver refinement (5 k*k doubles)
+  ttg::DevBuf eigf;           // FP32 tridiagonalisation scratch
   ttg::DevBuf partial;        // split-K partials for the Gram
   ttg::DevBuf scal;           // small FP64 scratch (reductions, status)
   ttg::DevBuf status;         // int32 device status words
@@ -121,15 +162,33 @@ ttg_status build_row_groups(ttg_op* op, int64_t n, const int64_t* hp, const int3
 ttg_status launch_cheb_step(ttg_op* op, int prec, const void* src, const void* xold,
                             void* dst, int k, double alpha, double beta, double delta);
 ttg_status launch_proj_w(ttg_op* op, int prec, void* src, int k);
+ttg_status launch_apply_df64(ttg_op* op, const double* src, double* dst, int k);
+
+// spmm_tc.cu
+ttg_status build_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int32_t* hc,
+                       const double* hv, int32_t nproj, const int64_t* cp, const int32_t* cc,
+                       const double* cv, const int32_t* dims);
+bool tc_supported(const ttg_op* op, int prec, int k);
+ttg_status launch_cheb_tc(ttg_op* op, int prec, const void* src, const void* xold, void* dst,
+                          int k, double alpha, double beta, double delta);
 ttg_status launch_convert(ttg_op* op, int from, int to, const void* src, void* dst,
                           int64_t rows, int k);
+
+// scf.cu: FP64 strided-batched GEMM (split-K when the output is small)
+struct DOp {
+  const double* p;
+  int64_t rs, cs, bs;   // element strides: row (m or k), column (k or n), batch
+};
+ttg_status dgemm(cudaStream_t st, int M, int N, int K, int batch, DOp A, DOp B, double* C,
+                 int64_t c_rs, int64_t c_cs, int64_t c_bs, DevBuf& scratch);
 
 // dense.cu
 ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* S);
 ttg_status gemm_nn_small(ttg_op* op, const double* X, const double* Q, double* out, int k,
                          int transQ);
 ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_status);
-ttg_status syev_jacobi(ttg_op* op, double* A, double* V, double* w, int k, int* d_status);
+ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* d_status);
+ttg_status sym_topk(ttg_op* op, double* A, int n, int r, double* w, double* U, int* d_status);
 ttg_status colmajor_to_rows(ttg_op* op, const double* src, int64_t ld_src, double* dst,
                             int64_t ld_dst, int64_t n, int k);
 ttg_status rows_to_colmajor(ttg_op* op, const double* src, int64_t ld_src, double* dst,

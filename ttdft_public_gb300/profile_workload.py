@@ -1,0 +1,49 @@
+"""Run a few hot-path launches of one workload, for profilers.
+
+    python -m ttdft_public_gb300.profile_workload --workload atoms64 \
+        --prec fp32,bf16 --degrees 1 [--rr]
+
+Builds the workload's operator, uploads a random block and runs `degrees`
+filter degrees per listed precision (one fused SpMM launch each) and, with
+--rr, one Rayleigh-Ritz projection (the df64 SpMM, Gram and eigensolve).  Few
+launches and no timing loop, so that an ncu capture of it stays small."""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+from ttdft_public_gb300 import api, system  # noqa: E402
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="atoms64", choices=sorted(system.CONFIGS))
+    ap.add_argument("--prec", default="fp32,bf16")
+    ap.add_argument("--degrees", type=int, default=1)
+    ap.add_argument("--rr", action="store_true")
+    args = ap.parse_args()
+    s = system.build_system(system.CONFIGS[args.workload],
+                            cache_dir=os.environ.get("TTG_CACHE"))
+    k = s.spec.n_states
+    op = api.Operator(api.ProjectHamiltonianSparse.from_system(s), k)
+    X = api.Mat(op, k, np.random.default_rng(0).standard_normal((s.N, k)))
+    ax = api.AX(1, k)
+    ax.op = op
+    lo, hi = -0.5, 20.0
+    for p in args.prec.split(","):
+        api.ChebyShevFilter(api.sched(p)).computeFilteredSubspace(None, ax, X, s.N, args.degrees,
+                                                                 0.0, hi, lo)
+    if args.rr:
+        api.MultTM().orth(X)
+        api.rayleigh_ritz(op, X, rotate=False)
+    op.sync()
+    print("profile_workload done:", op.info())
+
+
+if __name__ == "__main__":
+    main()

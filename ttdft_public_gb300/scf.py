@@ -1,0 +1,401 @@
+"""Kohn-Sham self-consistent field loop over the GB300 kernels.
+
+Restates the SCF driver of the reference (main.cc:846-1522) for the synthetic
+systems of system.py:
+
+  1. rho_in: the atomic-density guess on the first iteration
+     (InitialGuess, dft/InitialGuess.cc:573-681, normalised to N_e as at
+     main.cc:674-680), Anderson mixing afterwards (dft/AndersonMixing.cc:
+     150-374).
+  2. Hartree potential of rho_in through its Tucker form and the Gaussian
+     kernel expansion (main.cc:885-896, dft/KSDFTPotential.cc:269-340).
+  3. V_eff = V_loc + V_H + V_xc(LDA) (main.cc:936-946).
+  4. Tucker decomposition of V_eff and new values of H_loc (main.cc:951-972).
+  5. Chebyshev-filtered subspace iteration with the reference's restart and
+     bound logic (main.cc:977-1207).
+  6. Fermi level and occupations (main.cc:1239-1272).
+  7. rho_out on the nodes, Tucker-compressed, projected to the quadrature
+     points, |.| (ProjectHamiltonianSparse::computeRhoOut, .cc:911-1221).
+  8. Total energy with V_H(rho_out) (main.cc:1288-1401).
+
+Every grid operation runs on the GPU through libttg's C ABI; torch only holds
+device memory.  The system is made neutral by Gaussian ionic charges whose
+potential (erf(r/w)/r, exact) is part of V_loc; their point-charge repulsion
+is E_nn as in the reference (KSDFTEnergyFunctional::computeRepulsiveEnergy).
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import math
+import time
+
+import numpy as np
+
+from . import _lib, api
+from ._lib import check
+from .kernel_expansion import coulomb_expansion
+
+KB_HA_PER_K = 3.166811429e-6   # main.cc:174
+
+
+@dataclasses.dataclass
+class ScfConfig:
+    max_iter: int = 40
+    tol_e_atom: float = 1e-5          # |E_k - E_{k-1}| / n_atoms, Ha
+    mix_alpha: float = 0.5            # Anderson mixing parameter
+    history: int = 5                  # Anderson depth
+    temperature: float = 500.0        # K
+    rho_eps: float = 1e-4             # STHOSVD tolerance of the densities
+    rho_rank_cap: int = 64
+    veff_eps: float = 1e-7            # STHOSVD tolerance of V_eff
+    veff_rank_cap: int = 32
+    restarts_first: int = 10          # Chebyshev passes, first SCF step
+    restarts_other: int = 12          # Chebyshev passes, later steps
+    cheb_tol: float = 1e-3            # |d eps_occ / eps_occ| to stop the passes
+    lanczos_iter: int = 20
+    ion_width: float = 1.0            # Gaussian ionic charges (bohr)
+    sad_width: float = 1.0            # width of the atomic densities (bohr)
+    filter: str = "fp64"              # fp64 | fp32 | mixed (BF16 first quarter)
+    seed: int = 0
+
+
+def cheb_schedule(cfg: ScfConfig, m: int):
+    if cfg.filter == "fp64":
+        return api.sched("fp64")
+    if cfg.filter == "fp32":
+        return api.sched("fp32")
+    return api.sched("fp32", low="bf16", n_low=m // 4)
+
+
+def repulsive_energy(atoms, z):
+    """KSDFTEnergyFunctional::computeRepulsiveEnergy (.cc:126-141)."""
+    e = 0.0
+    for i in range(len(atoms)):
+        for j in range(i):
+            e += z * z / np.linalg.norm(atoms[i] - atoms[j])
+    return e
+
+
+def potential_matrices(basis, U):
+    """PX_a[i][j] = int psi_i u_a psi_j for factor columns u_a at the quad
+    points (ProjectHamiltonianSparse::computeOverlapPotentialTuckerBasis,
+    dft/ProjectHamiltonianSparse.cc:678-775); (r_a, r, r)."""
+    B = basis.quad * basis.fem.wJ[:, None]
+    return np.ascontiguousarray(np.einsum("qi,qa,qj->aij", B, U, basis.quad, optimize=True))
+
+
+class Scf:
+    """One SCF run of a system built by system.build_system on cuda:0."""
+
+    def __init__(self, sysm, cfg: ScfConfig | None = None, n_states: int | None = None,
+                 degree: int | None = None):
+        import torch
+        self.torch = torch
+        self.s = sysm
+        self.cfg = cfg or ScfConfig()
+        spec = sysm.spec
+        self.k = n_states or spec.n_states
+        self.m = degree or spec.degree
+        self.ne = spec.n_electrons
+        self.natoms = spec.n_atoms
+        self.lib = _lib.ttg()
+        self.dev = torch.device("cuda")
+        b = sysm.basis
+        self.fem = b[0].fem
+        self.q = [bb.fem.nq for bb in b]
+        self.nn = [bb.fem.n_nodes for bb in b]
+        self.qdims = np.array(self.q, np.int32)
+        self.ndims = np.array(self.nn, np.int32)
+        self.nq = int(np.prod(self.q))
+        H = api.ProjectHamiltonianSparse.from_system(sysm)
+        self.op = api.Operator(H, self.k)
+        mats = [bb.stiffness() for bb in b] + [bb.overlap() for bb in b]
+        mats = [np.ascontiguousarray(m_) for m_ in mats]
+        check(self.lib.ttg_op_set_kinetic(self.op.h, *[_lib.ptr(m_) for m_ in mats]),
+              "ttg_op_set_kinetic")
+        self.wq = [self._dev(bb.fem.wJ) for bb in b]
+        self.xq = [bb.fem.xq for bb in b]
+        self.alpha, self.omega = coulomb_expansion()
+        # fixed local potential: Gaussian wells + neutralising ionic charges
+        self.vloc = self._zeros()
+        fx = [np.stack([np.exp(-(self.xq[d] - a[d]) ** 2 / (2 * spec.sigma ** 2)) for a in sysm.atoms])
+              for d in range(3)]
+        self._cp_sum(-spec.z_val * np.ones(self.natoms), fx, self.vloc, self.qdims, accumulate=False)
+        pos = self._dev(np.ascontiguousarray(sysm.atoms))
+        zs = self._dev(np.full(self.natoms, spec.z_val))
+        check(self.lib.ttg_grid_ion_potential(self.natoms, self._p(pos), self._p(zs),
+                                              self.cfg.ion_width, *[self._p(self._dev(x)) for x in self.xq],
+                                              _lib.ptr(self.qdims), self._p(self.vloc), None),
+              "ttg_grid_ion_potential")
+        self.e_nn = repulsive_energy(sysm.atoms, spec.z_val)
+        self.timings = {}
+
+    # ---- small helpers -----------------------------------------------------
+    def _dev(self, a):
+        return self.torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.dev)
+
+    def _zeros(self, n=None):
+        return self.torch.zeros(n or self.nq, dtype=self.torch.float64, device=self.dev)
+
+    @staticmethod
+    def _p(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    def _cp_sum(self, coef, f, out, dims, accumulate):
+        c = self._dev(coef)
+        fd = [self._dev(np.ascontiguousarray(x)) for x in f]
+        check(self.lib.ttg_grid_cp_sum(len(coef), self._p(c), *[self._p(x) for x in fd],
+                                       _lib.ptr(dims), self._p(out), 1 if accumulate else 0, None),
+              "ttg_grid_cp_sum")
+
+    def integrate(self, f, g=None):
+        res = ctypes.c_double()
+        check(self.lib.ttg_grid_integrate(self._p(f), None if g is None else self._p(g),
+                                          _lib.ptr(self.qdims), *[self._p(w) for w in self.wq],
+                                          ctypes.byref(res), None), "ttg_grid_integrate")
+        return res.value
+
+    def lincomb(self, fields, coef, out, take_abs=False):
+        arr = (ctypes.c_void_p * len(fields))(*[f.data_ptr() for f in fields])
+        c = np.ascontiguousarray(coef, dtype=np.float64)
+        check(self.lib.ttg_grid_lincomb(len(fields), arr, _lib.ptr(c), out.numel(), self._p(out),
+                                        1 if take_abs else 0, None), "ttg_grid_lincomb")
+        return out
+
+    def sthosvd(self, field, dims, eps, cap):
+        """Tucker decomposition on the device; returns (core, [U_d]) on host."""
+        torch = self.torch
+        caps = np.array([min(cap, int(d)) for d in dims], np.int32)
+        core = torch.zeros(int(np.prod(caps)), dtype=torch.float64, device=self.dev)
+        U = [torch.zeros(int(dims[d]) * int(caps[d]), dtype=torch.float64, device=self.dev)
+             for d in range(3)]
+        ranks = np.zeros(3, np.int32)
+        check(self.lib.ttg_tucker_sthosvd(self.op.h, self._p(field), _lib.ptr(np.asarray(dims, np.int32)),
+                                          float(eps), _lib.ptr(caps), _lib.ptr(ranks), self._p(core),
+                                          *[self._p(u) for u in U]), "ttg_tucker_sthosvd")
+        r = [int(x) for x in ranks]
+        G = core[: r[0] * r[1] * r[2]].cpu().numpy()
+        Uh = [U[d][: int(dims[d]) * r[d]].cpu().numpy().reshape(r[d], int(dims[d])).T.copy()
+              for d in range(3)]
+        return G, Uh, r
+
+    def hartree(self, G, Uq, r):
+        """V_H on the quadrature grid from a Tucker density with factors at
+        the quad points (one launch over all expansion terms)."""
+        quad = [(self.xq[d], self.fem_w(d)) for d in range(3)]
+        V, ms = api.hartree(self.alpha, self.omega, G.reshape(r[2], r[1], r[0]), quad, Uq, self.xq)
+        self.timings["hartree_ms"] = self.timings.get("hartree_ms", 0.0) + ms
+        return self._dev(V.reshape(-1))
+
+    def hartree_energy(self, G, Uq, r):
+        quad = [(self.xq[d], self.fem_w(d)) for d in range(3)]
+        return api.hartree_energy(self.alpha, self.omega, G.reshape(r[2], r[1], r[0]), quad, Uq)
+
+    def fem_w(self, d):
+        return self.s.basis[d].fem.wJ
+
+    def reconstruct(self, G, U, r, dims):
+        torch = self.torch
+        core = self._dev(G)
+        Ud = [self._dev(np.asfortranarray(U[d]).reshape(-1, order="F")) for d in range(3)]
+        out = torch.zeros(int(np.prod(dims)), dtype=torch.float64, device=self.dev)
+        check(self.lib.ttg_tucker_reconstruct(self._p(core), _lib.ptr(np.array(r, np.int32)),
+                                              *[self._p(u) for u in Ud],
+                                              _lib.ptr(np.asarray(dims, np.int32)), self._p(out), None),
+              "ttg_tucker_reconstruct")
+        return out
+
+    # ---- SCF pieces -----------------------------------------------------------
+    def initial_density(self):
+        spec, cfg = self.s.spec, self.cfg
+        w = cfg.sad_width
+        norm = spec.z_val / (math.pi * w * w) ** 1.5
+        f = [np.stack([np.exp(-(self.xq[d] - a[d]) ** 2 / (w * w)) for a in self.s.atoms])
+             for d in range(3)]
+        rho = self._zeros()
+        self._cp_sum(norm * np.ones(self.natoms), f, rho, self.qdims, accumulate=False)
+        rho *= self.ne / self.integrate(rho)                       # main.cc:674-680
+        return rho
+
+    def veff_from(self, rho_in):
+        """V_eff = V_loc + V_H(rho_in) + V_xc(rho_in) on the quad grid."""
+        cfg = self.cfg
+        G, U, r = self.sthosvd(rho_in, self.qdims, cfg.rho_eps, cfg.rho_rank_cap)
+        vh = self.hartree(G, U, r)
+        veff = vh + self.vloc
+        check(self.lib.ttg_grid_lda(self._p(rho_in), self.nq, self._p(veff), None, 1, None),
+              "ttg_grid_lda")
+        return veff
+
+    def update_hamiltonian(self, veff):
+        G, U, r = self.sthosvd(veff, self.qdims, self.cfg.veff_eps, self.cfg.veff_rank_cap)
+        P = [potential_matrices(self.s.basis[d], U[d]) for d in range(3)]
+        check(self.lib.ttg_op_update_potential(self.op.h, _lib.ptr(np.array(r, np.int32)),
+                                               _lib.ptr(np.ascontiguousarray(G)),
+                                               *[_lib.ptr(p) for p in P]), "ttg_op_update_potential")
+        self.veff_ranks = r
+
+    def density_out(self, X, occ):
+        """computeRhoOut: nodal density, STHOSVD, factors projected to the
+        quadrature points, reconstruction, |.|; also returns the Tucker form
+        at the quad points for the Hartree term."""
+        rho_n = api.density(self.op, X, occ, self.s.basis).reshape(-1)
+        rho_nd = self._dev(rho_n)
+        G, U, r = self.sthosvd(rho_nd, self.ndims, self.cfg.rho_eps, self.cfg.rho_rank_cap)
+        Uq = [self.s.basis[d].fem.interp_matrix() @ U[d] for d in range(3)]
+        raw = self.reconstruct(G, Uq, r, self.qdims)
+        rho = self.lincomb([raw], [1.0], self._zeros(), take_abs=True)
+        return rho, (G, Uq, r, raw)
+
+    def run(self, callback=None, rho0=None):
+        cfg, torch = self.cfg, self.torch
+        k, m = self.k, self.m
+        kT = KB_HA_PER_K * cfg.temperature
+        X = api.Mat(self.op, k, np.random.default_rng(cfg.seed).standard_normal((self.s.N, k)))
+        v0 = np.random.default_rng(cfg.seed + 1).uniform(0, 1, self.s.N)
+        occ_idx = min(int(self.ne / 2.0 + 10), k - 1)               # main.cc:686-688
+        hist_in, hist_out = [], []
+        upper = 1e16
+        err_upper = 1e16
+        lower_wanted = lower_unwanted = None
+        occ_energy = 1e9
+        e_old = None
+        history = []
+        rho_in = self.initial_density() if rho0 is None else rho0
+        sch = cheb_schedule(cfg, m)
+        t_start = time.perf_counter()
+        w = None
+        for it in range(cfg.max_iter):
+            t_it = time.perf_counter()
+            ph = {}
+            mark = [t_it]
+
+            def lap(name):
+                torch.cuda.synchronize()
+                now = time.perf_counter()
+                ph[name] = ph.get(name, 0.0) + now - mark[0]
+                mark[0] = now
+
+            if it > 0:
+                rho_in = self.anderson(hist_in, hist_out)
+                lap("mixing")
+            veff = self.veff_from(rho_in)
+            lap("veff")
+            self.update_hamiltonian(veff)
+            lap("h_update")
+            # spectral bounds (main.cc:987-1014)
+            if err_upper > 0.01:
+                cur, tmp_lower = api.EigenSolver(self.op).computeUpperBoundWithLanczos(
+                    None, cfg.lanczos_iter, v0=v0)
+                err_upper = (upper - cur) / upper
+                upper = cur if err_upper > 0.01 else cur * 1.05
+                if it == 0:
+                    lower_wanted, lower_unwanted = tmp_lower, 0.0
+            lap("lanczos")
+            if it > 0:
+                lower_wanted, lower_unwanted = w[0], w[-1]
+            restarts = cfg.restarts_first if it == 0 else cfg.restarts_other
+            n_pass = 0
+            for _ in range(restarts):
+                n_pass += 1
+                w = api.chfsi_pass(self.op, X, m, lower_unwanted, upper, lower_wanted, sch,
+                                   rotate=True)
+                lower_wanted, lower_unwanted = w[0], w[-1]
+                cur_occ = w[occ_idx]
+                err = abs((cur_occ - occ_energy) / occ_energy)
+                occ_energy = cur_occ
+                if err < cfg.cheb_tol:
+                    break
+            lap("chfsi")
+            mu, occ = api.fermi(self.op, w, self.ne, kT)
+            lap("fermi")
+            rho_out, (G, Uq, r, raw) = self.density_out(X, occ)
+            lap("rho_out")
+            vh_out = self.hartree(G, Uq, r)
+            # 1/2 int |rho| V_H(rho): the Tucker part exactly in FP64, the
+            # |.| correction (of the size of the truncation) with the FP32 V_H
+            e_h = self.hartree_energy(G, Uq, r) + 0.5 * self.integrate(
+                self.lincomb([rho_out, raw], [1.0, -1.0], self._zeros()), vh_out)
+            # energy (main.cc:1315-1401)
+            e_band = float(np.sum(2.0 * occ * w))
+            exc = self._zeros()
+            check(self.lib.ttg_grid_lda(self._p(rho_out), self.nq, None, self._p(exc), 0, None),
+                  "ttg_grid_lda")
+            e_grid = (self.integrate(exc) + e_h
+                      - self.integrate(rho_out, veff) + self.integrate(rho_out, self.vloc))
+            energy = e_band + e_grid + self.e_nn
+            drho = self.lincomb([rho_out, rho_in], [1.0, -1.0], self._zeros())
+            drho2 = self.integrate(drho, drho)
+            lap("energy")
+            hist_in.append(rho_in)
+            hist_out.append(rho_out)
+            if len(hist_in) > cfg.history:
+                hist_in.pop(0)
+                hist_out.pop(0)
+            de = None if e_old is None else abs(energy - e_old) / self.natoms
+            rec = {"iter": it, "energy": energy, "e_atom": energy / self.natoms, "de_atom": de,
+                   "drho2": drho2, "fermi": mu, "eig_lowest": float(w[0]),
+                   "veff_ranks": list(self.veff_ranks), "s": time.perf_counter() - t_it,
+                   "phases": ph, "passes": n_pass}
+            history.append(rec)
+            if callback:
+                callback(rec)
+            e_old = energy
+            if de is not None and de < cfg.tol_e_atom:
+                break
+        torch.cuda.synchronize()
+        self.eigenvalues = w
+        self.X = X
+        self.rho = hist_out[-1]
+        return {"history": history, "energy": history[-1]["energy"],
+                "iterations": len(history), "converged": history[-1]["de_atom"] is not None
+                and history[-1]["de_atom"] < cfg.tol_e_atom,
+                "wall_s": time.perf_counter() - t_start}
+
+    def anderson(self, hin, hout):
+        """AndersonMixing::computeMixingConstants + computeRhoIn
+        (dft/AndersonMixing.cc:150-316): weighted least squares on the
+        residuals F = rho_out - rho_in, then |alpha rho_out_bar + (1-alpha) rho_in_bar|."""
+        h = len(hin)
+        F = [self.lincomb([hout[i], hin[i]], [1.0, -1.0], self._zeros()) for i in range(h)]
+        n = h - 1
+        A = np.zeros((n, n))
+        b = np.zeros(n)
+        Fn = F[h - 1]
+        D = [self.lincomb([Fn, F[h - 2 - mm]], [1.0, -1.0], self._zeros()) for mm in range(n)]
+        for mm in range(n):
+            for kk in range(n):
+                A[mm, kk] = self.integrate(D[mm], D[kk])
+            b[mm] = self.integrate(D[mm], Fn)
+        c = solve_small(A, b) if n > 0 else np.zeros(0)
+        # rho_in_bar = rho_in_n + sum c_k (rho_in_k - rho_in_n), same for out
+        fin = [hin[h - 1]] + [hin[h - 2 - kk] for kk in range(n)]
+        fout = [hout[h - 1]] + [hout[h - 2 - kk] for kk in range(n)]
+        cin = [1.0 - float(np.sum(c))] + [float(x) for x in c]
+        a = self.cfg.mix_alpha
+        fields = fin + fout
+        coef = [(1.0 - a) * x for x in cin] + [a * x for x in cin]
+        return self.lincomb(fields, coef, self._zeros(), take_abs=True)
+
+
+def solve_small(A, b):
+    """Gaussian elimination with partial pivoting for the <= history-1 sized
+    mixing system (the reference calls dgesv, AndersonMixing.cc:238-246)."""
+    A = np.array(A, dtype=float)
+    b = np.array(b, dtype=float)
+    n = len(b)
+    for i in range(n):
+        p = i + int(np.argmax(np.abs(A[i:, i])))
+        if A[p, i] == 0:
+            continue
+        A[[i, p]] = A[[p, i]]
+        b[[i, p]] = b[[p, i]]
+        for j in range(i + 1, n):
+            f = A[j, i] / A[i, i]
+            A[j, i:] -= f * A[i, i:]
+            b[j] -= f * b[i]
+    x = np.zeros(n)
+    for i in range(n - 1, -1, -1):
+        x[i] = (b[i] - A[i, i + 1:] @ x[i + 1:]) / A[i, i] if A[i, i] != 0 else 0.0
+    return x
