@@ -222,7 +222,8 @@ ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const d
 /* Sequentially truncated HOSVD (TuckerMPI::STHOSVD as used at main.cc:951-955
  * and tensor/TensorUtils.cc:245-264): per mode, the eigenvectors of the mode
  * Gram matrix, keeping the smallest rank whose discarded eigenvalues sum to
- * at most eps^2 ||T||^2 / 3 (capped by max_ranks when not NULL).  Outputs:
+ * at most eps^2 ||T||^2 / 3 (capped by max_ranks when not NULL); eps 0
+ * keeps exactly max_ranks (the fixed-rank form of main.cc:952-956).  Outputs:
  * ranks, core (x-fastest), factors u_d (n_d x r_d column-major) -- all device
  * buffers sized for the caps. */
 ttg_status ttg_tucker_sthosvd(ttg_op* op, const double* t_dev, const int32_t* dims, double eps,
@@ -258,7 +259,7 @@ ttg_status ttg_grid_ion_potential(int32_t natoms, const double* pos_dev, const d
                                   double width, const double* gx_dev, const double* gy_dev,
                                   const double* gz_dev, const int32_t* dims, double* out_dev,
                                   void* stream);
-/* out = sum_m coef[m] fields[m] (|.| when take_abs), up to 12 fields
+/* out = sum_m coef[m] fields[m] (|.| when take_abs), up to 24 fields
  * (dft/AndersonMixing.cc:267-316). */
 ttg_status ttg_grid_lincomb(int32_t nterms, const double* const* fields_dev, const double* coef,
                             int64_t n, double* out_dev, int32_t take_abs, void* stream);

@@ -22,7 +22,8 @@ from ttdft_public_gb300.system import Csr
 def sthosvd(T, eps, cap):
     """Sequentially truncated HOSVD of an x-fastest tensor given as (n2, n1, n0)
     array: per mode, eigenvectors of the mode Gram matrix, discarding the
-    smallest eigenvalues while their sum stays <= eps^2 |T|^2 / 3."""
+    smallest eigenvalues while their sum stays <= eps^2 |T|^2 / 3 (eps 0: the
+    rank is the cap, as the fixed-rank STHOSVD of main.cc:952-956)."""
     A = np.transpose(T, (2, 1, 0)).copy()          # (n0, n1, n2): mode d = axis d
     thr = eps * eps * float(np.sum(A * A)) / 3.0
     U = []
@@ -36,7 +37,7 @@ def sthosvd(T, eps, cap):
                 break
             disc += lam
             r = len(w) - i - 1
-        r = max(1, min(r, cap))
+        r = max(1, min(r if eps > 0 else len(w), cap))     # eps 0: exactly the cap
         Ud = V[:, ::-1][:, :r]
         U.append(Ud)
         A = np.moveaxis(np.tensordot(Ud.T, np.moveaxis(A, d, 0), axes=(1, 0)), 0, d)
@@ -134,18 +135,26 @@ class OracleScf:
         core, U = sthosvd(veff, self.cfg.veff_eps, self.cfg.veff_rank_cap)
         P = [potential_matrices(self.s.basis[d], U[d]) for d in range(3)]
         (xi, yi, zi), (xj, yj, zj) = self.I3, self.J3
-        A = P[0][:, xi, xj].T
-        B = P[1][:, yi, yj].T
-        C = P[2][:, zi, zj].T
-        T = np.einsum("ea,abc->ebc", A, core, optimize=True)
-        T = np.einsum("eb,ebc->ec", B, T, optimize=True)
-        vals = self.kin + np.einsum("ec,ec->e", C, T)
+        # sum_abc core[a,b,c] P0[a,xi,xj] P1[b,yi,yj] P2[c,zi,zj] over the
+        # pattern: the (y, z) pair part tabulated once, entries in chunks
+        r = self.r
+        ypair, yinv = np.unique(yi * r[1] + yj, return_inverse=True)
+        zpair, zinv = np.unique(zi * r[2] + zj, return_inverse=True)
+        B = P[1][:, ypair // r[1], ypair % r[1]]                 # (rb, ny)
+        C = P[2][:, zpair // r[2], zpair % r[2]]                 # (rc, nz)
+        Q = np.einsum("abc,bj,ck->jka", core, B, C, optimize=True)
+        vals = self.kin.copy()
+        step = 1 << 18
+        for s0 in range(0, vals.size, step):
+            e = slice(s0, s0 + step)
+            A = P[0][:, xi[e], xj[e]]                            # (ra, chunk)
+            vals[e] += np.einsum("ae,ea->e", A, Q[yinv[e], zinv[e]])
         H = self.s.H
         return Csr(H.n_rows, H.n_cols, H.row_ptr, H.col, vals)
 
     def density_out(self, X, occ):
         rho_n = oracle.density(X, occ, self.s.basis)
-        core, U = sthosvd(rho_n, self.cfg.rho_eps, self.cfg.rho_rank_cap)
+        core, U = sthosvd(rho_n, self.cfg.rho_out_eps, self.cfg.rho_out_rank_cap)
         Uq = [self.s.basis[d].fem.interp_matrix() @ U[d] for d in range(3)]
         return np.abs(reconstruct(core, Uq)), (core, Uq)
 

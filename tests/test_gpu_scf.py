@@ -140,3 +140,24 @@ def test_scf_converges_and_precisions_agree(scf_system):
         assert res["converged"], mode
         e[mode] = res["energy"]
     assert abs(e["fp64"] - e["mixed"]) / scf_system.spec.n_atoms < 1e-5
+
+
+def test_sthosvd_degenerate_spectrum_fixed_rank(gpu_scf):
+    """Fixed-rank STHOSVD past the exact rank: a repeated singular value and
+    zero-eigenvalue directions (nearly parallel inverse-iteration vectors, the
+    Gram-Schmidt fallback of the orthonormalisation)."""
+    rng = np.random.default_rng(7)
+    n = (30, 26, 28)
+    U = [np.linalg.qr(rng.standard_normal((n[d], 3)))[0] for d in range(3)]
+    core = np.zeros((3, 3, 3))
+    core[0, 0, 0] = core[1, 1, 1] = 1.0
+    core[2, 2, 2] = 1e-6
+    T = oscf.reconstruct(core, U)
+    G, Ug, r = gpu_scf.sthosvd(gpu_scf._dev(T.reshape(-1)), np.array(n, np.int32), 0.0, 8)
+    assert list(r) == [8, 8, 8]
+    for d in range(3):
+        assert np.abs(Ug[d].T @ Ug[d] - np.eye(8)).max() < 1e-12
+    rec = oscf.reconstruct(G.reshape(r[2], r[1], r[0]).transpose(2, 1, 0), Ug)
+    # the 1e-6 component's Gram eigenvalue is 1e-12 of the largest, so its
+    # eigenvector carries ~1e-4 error from FP64 rounding of the Gram matrix
+    assert np.abs(rec - T).max() < 1e-9 * np.abs(T).max()

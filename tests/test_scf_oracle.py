@@ -75,3 +75,17 @@ def test_hartree_energy_identity():
     ref = 0.5 * float(np.sum(W * rho * V))
     e = oracle.hartree_energy(a, w, G, quad, U)
     assert abs(e - ref) < 1e-12 * abs(ref)
+
+
+def test_oracle_hamiltonian_values(tiny_system):
+    """H values of the oracle (pair tables, chunked) against the direct sum
+    H_e = kin_e + sum_abc core[a,b,c] P0[a,xi,xj] P1[b,yi,yj] P2[c,zi,zj]."""
+    c = oscf.OracleScf(tiny_system, scf.ScfConfig())
+    veff = c.veff_from(c.initial_density())
+    H = c.hamiltonian(veff)
+    core, U = oscf.sthosvd(veff, c.cfg.veff_eps, c.cfg.veff_rank_cap)
+    P = [scf.potential_matrices(tiny_system.basis[d], U[d]) for d in range(3)]
+    (xi, yi, zi), (xj, yj, zj) = c.I3, c.J3
+    ref = c.kin + np.einsum("abc,ae,be,ce->e", core, P[0][:, xi, xj], P[1][:, yi, yj],
+                            P[2][:, zi, zj], optimize=True)
+    assert np.abs(H.val - ref).max() < 1e-12 * np.abs(ref).max()

@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv(double* A, double* Linv, 
   }
 }
 
-// Symmetric eigensolver in two stages, one CTA, FP64:
+// Symmetric eigensolver in two stages, one CTA (run in FP32 here):
 //  (1) Householder reduction to tridiagonal form, A = Q T Q^T: for each
 //      column j, v = x - alpha e1 with x = A[j+1:, j], P = I - tau v v^T and
 //      the trailing block is updated as B <- P B P = B - v w^T - w v^T with
@@ -214,19 +214,22 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv(double* A, double* Linv, 
 //      each sweep's plane rotations, all threads then applying them to their
 //      own rows of Q.
 // 4n^3/3 flops for (1) plus O(n^2) rotations on Q in (2), against ~10
-// sweeps of 3n^3 for Jacobi.  status[0]: 0 ok, 1 QL did not converge.
-template <typename T, bool DO_QL = true>
+// sweeps of 3n^3 for Jacobi.  The vectors, the tridiagonal and the rotations
+// live in shared memory (6n elements, dynamic): the QL recurrence is a serial
+// chain of dependent accesses.  status[0]: 0 ok, 1 QL did not converge.
+template <typename T>
 __global__ void __launch_bounds__(1024) k_tridiag_ql(T* A, T* Q, T* w, int n, int* status,
                                                      T* scratch) {
   const T kTiny = sizeof(T) == 4 ? T(1.2e-7) : T(1e-16);
   __shared__ T red[32];
   __shared__ T s_alpha, s_tau;
-  T* v = scratch;               // n
-  T* p = scratch + n;           // n
-  T* d = scratch + 2 * n;       // n
-  T* e = scratch + 3 * n;       // n
-  T* vs = scratch + 4 * n;      // n*n: reflectors, column j holds v_j (rows j+1..)
-  T* rot = vs + (int64_t)n * n; // 2n: (c, s) of one QL sweep
+  extern __shared__ __align__(16) unsigned char ql_smem[];
+  T* v = reinterpret_cast<T*>(ql_smem);   // n
+  T* p = v + n;                 // n
+  T* d = p + n;                 // n
+  T* e = d + n;                 // n
+  T* rot = e + n;               // 2n: (c, s) of one QL sweep
+  T* vs = scratch;              // n*n: reflectors, column j holds v_j (rows j+1..)
   const int tid = threadIdx.x, nt = blockDim.x;
   // ---- (1) tridiagonalisation
   for (int j = 0; j + 2 < n; ++j) {
@@ -312,10 +315,6 @@ __global__ void __launch_bounds__(1024) k_tridiag_ql(T* A, T* Q, T* w, int n, in
     }
     __syncthreads();
   }
-  if constexpr (!DO_QL) {
-    if (tid == 0) status[0] = 0;
-    return;
-  }
   // ---- (2) implicit QL on (d, e), rotations applied to the rows of Q
   __shared__ int s_m, s_done, s_fail, s_nrot;
   __shared__ T s_floor;
@@ -399,118 +398,6 @@ __global__ void __launch_bounds__(1024) k_tridiag_ql(T* A, T* Q, T* w, int n, in
   }
   for (int i = tid; i < n; i += nt) w[i] = d[i];
   if (tid == 0) status[0] = s_fail;
-}
-
-// Largest r eigenpairs of a symmetric tridiagonal T (d, e: e[i] couples i and
-// i+1), FP64, one CTA.  Eigenvalues by bisection on Sturm counts, one thread
-// per eigenvalue, to full FP64 resolution (Gershgorin start interval);
-// eigenvectors by two steps of inverse iteration with a tridiagonal LU
-// (partial pivoting), then modified Gram-Schmidt in index order, which
-// separates the vectors of close eigenvalues.  Z is n x r column-major, w
-// descending.  Work space per thread: 4n doubles in `work`.
-__global__ void __launch_bounds__(256) k_tridiag_topk(const double* __restrict__ d,
-                                                      const double* __restrict__ e, int n, int r,
-                                                      double* __restrict__ w, double* Z,
-                                                      double* work) {
-  __shared__ double red[32];
-  __shared__ double s_lo, s_hi;
-  const int tid = threadIdx.x;
-  if (tid == 0) {
-    double lo = 1e300, hi = -1e300;
-    for (int i = 0; i < n; ++i) {
-      const double rad = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
-      lo = fmin(lo, d[i] - rad);
-      hi = fmax(hi, d[i] + rad);
-    }
-    const double pad = 1e-14 * fmax(fabs(lo), fabs(hi)) + 1e-300;
-    s_lo = lo - pad;
-    s_hi = hi + pad;
-  }
-  __syncthreads();
-  const double tnorm = fmax(fabs(s_lo), fabs(s_hi));
-  const double tiny = 1e-300;
-  for (int j = tid; j < r; j += blockDim.x) {
-    // eigenvalue index (ascending) n-1-j: count(x) = #eigenvalues < x
-    const int target = n - 1 - j;
-    double lo = s_lo, hi = s_hi;
-    for (int it = 0; it < 200 && hi - lo > 2.2e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300; ++it) {
-      const double x = 0.5 * (lo + hi);
-      int cnt = 0;
-      double q = d[0] - x;
-      if (q < 0) ++cnt;
-      for (int i = 1; i < n; ++i) {
-        if (fabs(q) < tiny) q = -tiny;
-        q = d[i] - x - e[i - 1] * e[i - 1] / q;
-        if (q < 0) ++cnt;
-      }
-      if (cnt > target) hi = x; else lo = x;
-    }
-    const double lam = 0.5 * (lo + hi);
-    w[j] = lam;
-    // inverse iteration: (T - lam I) z = b, LU with partial pivoting
-    double* dg = work + (int64_t)j * 4 * n;      // diagonal of U
-    double* u1 = dg + n;                         // first superdiagonal of U
-    double* u2 = u1 + n;                         // second superdiagonal (from pivoting)
-    double* z = u2 + n;                          // rhs / solution
-    for (int i = 0; i < n; ++i) z[i] = 1.0 / sqrt((double)n) * (1.0 + 0.01 * ((i * 7 + j * 13) % 17));
-    const double shift_guard = 1e-15 * tnorm + 1e-300;
-    for (int pass = 0; pass < 3; ++pass) {
-      // factor (T - lam I) = P L U, rows processed top-down; b transformed on the fly
-      double a = d[0] - lam, b = (n > 1 ? e[0] : 0.0), c = 0.0;   // current row: a, b, c
-      double zc = z[0];
-      for (int i = 0; i + 1 < n; ++i) {
-        const double sub = e[i];                 // T[i+1][i]
-        const double na = d[i + 1] - lam, nb = (i + 2 < n ? e[i + 1] : 0.0);
-        double zn = z[i + 1];
-        if (fabs(a) >= fabs(sub)) {
-          const double m = (fabs(a) > 0 ? sub / a : 0.0);
-          dg[i] = a; u1[i] = b; u2[i] = c;
-          a = na - m * b; b = nb - m * c; c = 0.0;
-          zn -= m * zc;
-        } else {
-          const double m = a / sub;              // swap rows i and i+1
-          dg[i] = sub; u1[i] = na; u2[i] = nb;
-          const double t = zc; zc = zn; zn = t - m * zn;
-          a = b - m * na; b = c - m * nb; c = 0.0;
-        }
-        z[i] = zc;
-        zc = zn;
-      }
-      dg[n - 1] = a;
-      z[n - 1] = zc;
-      // back substitution
-      for (int i = n - 1; i >= 0; --i) {
-        double v = z[i];
-        if (i + 1 < n) v -= u1[i] * z[i + 1];
-        if (i + 2 < n) v -= u2[i] * z[i + 2];
-        const double piv = fabs(dg[i]) > shift_guard ? dg[i] : (dg[i] >= 0 ? shift_guard : -shift_guard);
-        z[i] = v / piv;
-      }
-      double nrm = 0.0;
-      for (int i = 0; i < n; ++i) nrm += z[i] * z[i];
-      nrm = 1.0 / sqrt(nrm);
-      for (int i = 0; i < n; ++i) z[i] *= nrm;
-    }
-  }
-  __syncthreads();
-  // modified Gram-Schmidt over the r vectors in index order (block-parallel)
-  for (int j = 0; j < r; ++j) {
-    double* zj = work + (int64_t)j * 4 * n + 3 * n;
-    for (int i2 = 0; i2 < j; ++i2) {
-      const double* zi = Z + (int64_t)i2 * n;
-      double dot = 0.0;
-      for (int t = tid; t < n; t += blockDim.x) dot += zi[t] * zj[t];
-      dot = block_sum(dot, red);
-      for (int t = tid; t < n; t += blockDim.x) zj[t] -= dot * zi[t];
-      __syncthreads();
-    }
-    double nn = 0.0;
-    for (int t = tid; t < n; t += blockDim.x) nn += zj[t] * zj[t];
-    nn = block_sum(nn, red);
-    const double inv = 1.0 / sqrt(nn);
-    for (int t = tid; t < n; t += blockDim.x) Z[(int64_t)j * n + t] = zj[t] * inv;
-    __syncthreads();
-  }
 }
 
 // Sort eigenpairs ascending (stable rank sort), normalise each eigenvector's
@@ -791,7 +678,16 @@ ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* 
     TTG_TRY(op->eigf.alloc((size_t)(kk + 6 * (int64_t)k + 64) * sizeof(float)));
   k_d2f_vec<<<64, 256, 0, st>>>(A, Af, kk);
   TTG_LAUNCHED(op);
-  k_tridiag_ql<float><<<1, 1024, 0, st>>>(Af, Qf, wf, k, d_status, op->eigf.as<float>());
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(k_tridiag_ql<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    6 * 4096 * (int)sizeof(float));
+  });
+  if (attr_err != cudaSuccess) return TTG_CUDA_ERR;
+  if (k > 4096) return TTG_BAD_ARG;
+  k_tridiag_ql<float><<<1, 1024, 6 * k * sizeof(float), st>>>(Af, Qf, wf, k, d_status,
+                                                              op->eigf.as<float>());
   TTG_LAUNCHED(op);
   k_f2d_vec<<<64, 256, 0, st>>>(Qf, Vd, kk);
   TTG_LAUNCHED(op);
@@ -812,35 +708,6 @@ ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* 
   }
   k_sort_eig<<<(k + 127) / 128, 128, 0, st>>>(wtmp, Vd, w, V, k);
   TTG_LAUNCHED(op);
-  return TTG_OK;
-}
-
-// Largest r eigenpairs (descending) of a symmetric n x n column-major A, FP64:
-// Householder tridiagonalisation, bisection + inverse iteration on T, back-
-// transform U = Q Z.  w (r), U (n x r column-major) on the device; also the
-// trace of A into *trace_dev.
-ttg_status sym_topk(ttg_op* op, double* A, int n, int r, double* w, double* U, int* d_status) {
-  if (r < 1 || r > n) return TTG_BAD_ARG;
-  const int64_t nn = (int64_t)n * n;
-  const size_t need = (size_t)(2 * nn + 6 * (int64_t)n + 64 + (int64_t)r * (4 * n + n)) * sizeof(double);
-  if (op->eigbuf.bytes < need) TTG_TRY(op->eigbuf.alloc(need));
-  cudaStream_t st = op->stream;
-  double* Q = op->eigbuf.as<double>();
-  double* scratch = Q + nn;                         // v p d e | reflectors (n*n) | rot
-  double* Zt = scratch + nn + 6 * (int64_t)n + 64;  // r x n (tridiagonal basis)
-  double* work = Zt + (int64_t)r * n;               // r x 4n
-  k_symmetrize<<<64, 256, 0, st>>>(A, n);
-  TTG_LAUNCHED(op);
-  k_tridiag_ql<double, false><<<1, 1024, 0, st>>>(A, Q, w, n, d_status, scratch);
-  TTG_LAUNCHED(op);
-  const double* d = scratch + 2 * n;
-  const double* e = scratch + 3 * n;
-  k_tridiag_topk<<<1, 256, 0, st>>>(d, e, n, r, w, Zt, work);
-  TTG_LAUNCHED(op);
-  // U = Q Zt  (n x n)(n x r)
-  TTG_TRY(dgemm(st, n, r, n, 1, DOp{Q, 1, (int64_t)n, 0}, DOp{Zt, 1, (int64_t)n, 0}, U, 1, n, 0,
-                op->partial));
-  op->launches += 2;
   return TTG_OK;
 }
 

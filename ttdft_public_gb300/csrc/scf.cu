@@ -354,9 +354,10 @@ __global__ void k_diag_sum(const double* __restrict__ A, int n, double* out) {
   }
 }
 
+constexpr int kMaxLinTerms = 24;   // Anderson depth 10: 2 x 11 fields
 struct LinTerms {
-  const double* f[12];
-  double c[12];
+  const double* f[kMaxLinTerms];
+  double c[kMaxLinTerms];
 };
 
 __global__ void k_lincomb(LinTerms t, int nt, int64_t n, double* out, int take_abs) {
@@ -405,7 +406,7 @@ ttg_status ttg_tucker_sthosvd(ttg_op* op, const double* t_dev, const int32_t* di
     return TTG_BAD_ARG;
   int n[3] = {dims[0], dims[1], dims[2]};
   for (int d = 0; d < 3; ++d)
-    if (n[d] <= 0 || n[d] > 4096) return TTG_BAD_ARG;
+    if (n[d] <= 0 || n[d] > 2048) return TTG_BAD_ARG;
   cudaStream_t st = op->stream;
   const int64_t total = (int64_t)n[0] * n[1] * n[2];
   DevBuf A, B, gram, part, part2, norm;
@@ -453,9 +454,9 @@ ttg_status ttg_tucker_sthosvd(ttg_op* op, const double* t_dev, const int32_t* di
     if (stat) return TTG_NOT_CONVERGED;
     const double trace = w[rcap];
     // smallest r whose discarded eigenvalues sum to <= thr
-    int r = rcap;
+    int r = rcap;   // eps 0: fixed rank
     double kept = 0.0;
-    for (int i = 0; i < rcap; ++i) {
+    for (int i = 0; i < rcap && thr > 0.0; ++i) {
       kept += std::max(w[i], 0.0);
       if (trace - kept <= thr) {
         r = i + 1;
@@ -639,7 +640,7 @@ ttg_status ttg_grid_ion_potential(int32_t natoms, const double* pos_dev, const d
 
 ttg_status ttg_grid_lincomb(int32_t nterms, const double* const* fields_dev, const double* coef,
                             int64_t n, double* out_dev, int32_t take_abs, void* stream) {
-  if (nterms <= 0 || nterms > 12 || !fields_dev || !coef || !out_dev || n <= 0) return TTG_BAD_ARG;
+  if (nterms <= 0 || nterms > kMaxLinTerms || !fields_dev || !coef || !out_dev || n <= 0) return TTG_BAD_ARG;
   Stream S(stream);
   LinTerms t{};
   for (int m = 0; m < nterms; ++m) {

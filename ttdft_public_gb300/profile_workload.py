@@ -2,11 +2,14 @@
 
     python -m ttdft_public_gb300.profile_workload --workload atoms64 \
         --prec fp32,bf16 --degrees 1 [--rr]
+    python -m ttdft_public_gb300.profile_workload --workload atoms64 --scf 1 \
+        [--filter mixed]
 
 Builds the workload's operator, uploads a random block and runs `degrees`
 filter degrees per listed precision (one fused SpMM launch each) and, with
 --rr, one Rayleigh-Ritz projection (the df64 SpMM, Gram and eigensolve).  Few
-launches and no timing loop, so that an ncu capture of it stays small."""
+launches and no timing loop, so that an ncu capture of it stays small.  With
+--scf N it runs N iterations of the SCF loop instead (for launch lists)."""
 from __future__ import annotations
 
 import argparse
@@ -26,9 +29,18 @@ def main():
     ap.add_argument("--prec", default="fp32,bf16")
     ap.add_argument("--degrees", type=int, default=1)
     ap.add_argument("--rr", action="store_true")
+    ap.add_argument("--scf", type=int, default=0)
+    ap.add_argument("--filter", default="mixed", choices=("fp64", "fp32", "mixed"))
     args = ap.parse_args()
     s = system.build_system(system.CONFIGS[args.workload],
                             cache_dir=os.environ.get("TTG_CACHE"))
+    if args.scf:
+        from ttdft_public_gb300 import scf
+        res = scf.Scf(s, scf.ScfConfig(max_iter=args.scf, filter=args.filter)).run()
+        for h in res["history"]:
+            print("iter", h["iter"], "energy", h["energy"], "s", round(h["s"], 3),
+                  {k: round(v, 3) for k, v in h["phases"].items()})
+        return
     k = s.spec.n_states
     op = api.Operator(api.ProjectHamiltonianSparse.from_system(s), k)
     X = api.Mat(op, k, np.random.default_rng(0).standard_normal((s.N, k)))

@@ -46,10 +46,15 @@ class ScfConfig:
     mix_alpha: float = 0.5            # Anderson mixing parameter
     history: int = 5                  # Anderson depth
     temperature: float = 500.0        # K
-    rho_eps: float = 1e-4             # STHOSVD tolerance of the densities
-    rho_rank_cap: int = 64
-    veff_eps: float = 1e-7            # STHOSVD tolerance of V_eff
-    veff_rank_cap: int = 32
+    # Tucker ranks (main.cc:886-892, 952-956; ProjectHamiltonianSparse.cc:
+    # 1113-1118): rho_in for the Hartree term and V_eff at fixed ranks, rho_out
+    # at tolerance 1e-4.  eps 0 = exactly the rank (capped by the dimension).
+    rho_eps: float = 0.0
+    rho_rank_cap: int = 60
+    veff_eps: float = 0.0
+    veff_rank_cap: int = 72
+    rho_out_eps: float = 1e-4
+    rho_out_rank_cap: int = 96
     restarts_first: int = 10          # Chebyshev passes, first SCF step
     restarts_other: int = 12          # Chebyshev passes, later steps
     cheb_tol: float = 1e-3            # |d eps_occ / eps_occ| to stop the passes
@@ -242,7 +247,7 @@ class Scf:
         at the quad points for the Hartree term."""
         rho_n = api.density(self.op, X, occ, self.s.basis).reshape(-1)
         rho_nd = self._dev(rho_n)
-        G, U, r = self.sthosvd(rho_nd, self.ndims, self.cfg.rho_eps, self.cfg.rho_rank_cap)
+        G, U, r = self.sthosvd(rho_nd, self.ndims, self.cfg.rho_out_eps, self.cfg.rho_out_rank_cap)
         Uq = [self.s.basis[d].fem.interp_matrix() @ U[d] for d in range(3)]
         raw = self.reconstruct(G, Uq, r, self.qdims)
         rho = self.lincomb([raw], [1.0], self._zeros(), take_abs=True)
@@ -297,6 +302,7 @@ class Scf:
                 lower_wanted, lower_unwanted = w[0], w[-1]
             restarts = cfg.restarts_first if it == 0 else cfg.restarts_other
             n_pass = 0
+            errs = []
             for _ in range(restarts):
                 n_pass += 1
                 w = api.chfsi_pass(self.op, X, m, lower_unwanted, upper, lower_wanted, sch,
@@ -305,6 +311,7 @@ class Scf:
                 cur_occ = w[occ_idx]
                 err = abs((cur_occ - occ_energy) / occ_energy)
                 occ_energy = cur_occ
+                errs.append(float(err))
                 if err < cfg.cheb_tol:
                     break
             lap("chfsi")
@@ -337,7 +344,8 @@ class Scf:
             rec = {"iter": it, "energy": energy, "e_atom": energy / self.natoms, "de_atom": de,
                    "drho2": drho2, "fermi": mu, "eig_lowest": float(w[0]),
                    "veff_ranks": list(self.veff_ranks), "s": time.perf_counter() - t_it,
-                   "phases": ph, "passes": n_pass}
+                   "phases": ph, "passes": n_pass, "cheb_err": errs, "rho_ranks": list(r), "eig_top": float(w[-1]),
+                   "upper": upper, "n_out": self.integrate(rho_out)}
             history.append(rec)
             if callback:
                 callback(rec)
@@ -369,6 +377,7 @@ class Scf:
                 A[mm, kk] = self.integrate(D[mm], D[kk])
             b[mm] = self.integrate(D[mm], Fn)
         c = solve_small(A, b) if n > 0 else np.zeros(0)
+        self.mix_coef = c
         # rho_in_bar = rho_in_n + sum c_k (rho_in_k - rho_in_n), same for out
         fin = [hin[h - 1]] + [hin[h - 2 - kk] for kk in range(n)]
         fout = [hout[h - 1]] + [hout[h - 2 - kk] for kk in range(n)]
