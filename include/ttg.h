@@ -81,6 +81,9 @@ typedef struct {
 const char* ttg_version(void);
 ttg_status ttg_device_query(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
 const char* ttg_status_string(ttg_status s);
+/* Number of kernels this library has launched in the process so far (all
+ * entry points, all operators).  No counterpart in the reference. */
+int64_t ttg_kernel_launches(void);
 
 /* Upload the projected Hamiltonian.  Replaces AX::AX + AX::setup_system +
  * AX::setup_mata_on_device (eigensolver/Mult.h:37-44,

@@ -104,6 +104,7 @@ _OTHER = {
     "ttg_status_string": ([ctypes.c_int], ctypes.c_char_p),
     "ttg_op_stream": ([c_vp], c_vp),
     "ttg_block_cols": ([c_vp], c_i32),
+    "ttg_kernel_launches": ([], c_i64),
 }
 
 EXPORTED = sorted(list(_SIGS) + list(_OTHER))

@@ -46,9 +46,17 @@ ttg_status check_block(const ttg_op* op, const ttg_block* b) {
 
 }  // namespace
 
+namespace ttg {
+std::atomic<long long> g_kernel_launches{0};
+}
+
 extern "C" {
 
 const char* ttg_version(void) { return "ttg 0.1 (sm_103a)"; }
+
+int64_t ttg_kernel_launches(void) {
+  return (int64_t)ttg::g_kernel_launches.load(std::memory_order_relaxed);
+}
 
 const char* ttg_status_string(ttg_status s) {
   switch (s) {

@@ -624,11 +624,11 @@ ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* 
   if ((int64_t)op->partial.bytes < need) TTG_TRY(op->partial.alloc(need));
   const int64_t rows = (op->n + nsplit - 1) / nsplit;
   k_gram_tn<<<dim3(tp, tq, (unsigned)nsplit), 256, 0, op->stream>>>(X, Y, op->n, k, op->ld, rows,
-                                                                   op->partial.as<double>());
+                                                                   op->partial.as<double>()); TTG_COUNT();
   TTG_LAUNCHED(op);
   const int64_t kk = (int64_t)k * k;
   k_reduce_splits<<<(unsigned)std::min<int64_t>((kk + 255) / 256, 1024), 256, 0, op->stream>>>(
-      op->partial.as<double>(), (int)nsplit, kk, S);
+      op->partial.as<double>(), (int)nsplit, kk, S); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
@@ -636,13 +636,13 @@ ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* 
 ttg_status gemm_nn_small(ttg_op* op, const double* X, const double* Q, double* out, int k,
                          int transQ) {
   dim3 grid((unsigned)((op->n + TM - 1) / TM), (unsigned)((k + TN - 1) / TN));
-  k_gemm_nn<<<grid, 256, 0, op->stream>>>(X, Q, out, op->n, k, op->ld, transQ);
+  k_gemm_nn<<<grid, 256, 0, op->stream>>>(X, Q, out, op->n, k, op->ld, transQ); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
 
 ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_status) {
-  k_cholesky_inv<<<1, 1024, 0, op->stream>>>(S, Linv, k, d_status);
+  k_cholesky_inv<<<1, 1024, 0, op->stream>>>(S, Linv, k, d_status); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
@@ -669,14 +669,14 @@ ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* 
   float* Af = op->kk3.as<float>();
   float* Qf = Af + kk;
   float* wf = Qf + kk;
-  k_symmetrize<<<64, 256, 0, st>>>(A, k);
+  k_symmetrize<<<64, 256, 0, st>>>(A, k); TTG_COUNT();
   TTG_LAUNCHED(op);
-  k_frob2<<<1, 1024, 0, st>>>(A, kk, normA);
+  k_frob2<<<1, 1024, 0, st>>>(A, kk, normA); TTG_COUNT();
   TTG_LAUNCHED(op);
   // FP32 stage: Af <- A; tridiagonalise + QL (scratch: vectors + reflectors)
   if (op->eigf.bytes < (size_t)(kk + 6 * (int64_t)k + 64) * sizeof(float))
     TTG_TRY(op->eigf.alloc((size_t)(kk + 6 * (int64_t)k + 64) * sizeof(float)));
-  k_d2f_vec<<<64, 256, 0, st>>>(A, Af, kk);
+  k_d2f_vec<<<64, 256, 0, st>>>(A, Af, kk); TTG_COUNT();
   TTG_LAUNCHED(op);
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
@@ -687,9 +687,9 @@ ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* 
   if (attr_err != cudaSuccess) return TTG_CUDA_ERR;
   if (k > 4096) return TTG_BAD_ARG;
   k_tridiag_ql<float><<<1, 1024, 6 * k * sizeof(float), st>>>(Af, Qf, wf, k, d_status,
-                                                              op->eigf.as<float>());
+                                                              op->eigf.as<float>()); TTG_COUNT();
   TTG_LAUNCHED(op);
-  k_f2d_vec<<<64, 256, 0, st>>>(Qf, Vd, kk);
+  k_f2d_vec<<<64, 256, 0, st>>>(Qf, Vd, kk); TTG_COUNT();
   TTG_LAUNCHED(op);
   const DOp Vt{Vd, (int64_t)k, 1, 0}, Vn{Vd, 1, (int64_t)k, 0}, An{A, 1, (int64_t)k, 0};
   for (int it = 0; it <= 2; ++it) {
@@ -698,15 +698,15 @@ ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* 
     TTG_TRY(dgemm(st, k, k, k, 1, Vt, DOp{AV, 1, (int64_t)k, 0}, Sm, 1, k, 0,
                   op->partial));                                                // S = V^T A V
     op->launches += 6;
-    k_oa_step<<<1, 1024, 0, st>>>(Gm, Sm, k, normA, E, wtmp);
+    k_oa_step<<<1, 1024, 0, st>>>(Gm, Sm, k, normA, E, wtmp); TTG_COUNT();
     TTG_LAUNCHED(op);
     if (it == 2) break;                                                        // final lam only
     TTG_TRY(dgemm(st, k, k, k, 1, Vn, DOp{E, 1, (int64_t)k, 0}, VE, 1, k, 0, op->partial));
     op->launches += 2;
-    k_add<<<64, 256, 0, st>>>(Vd, VE, kk);
+    k_add<<<64, 256, 0, st>>>(Vd, VE, kk); TTG_COUNT();
     TTG_LAUNCHED(op);
   }
-  k_sort_eig<<<(k + 127) / 128, 128, 0, st>>>(wtmp, Vd, w, V, k);
+  k_sort_eig<<<(k + 127) / 128, 128, 0, st>>>(wtmp, Vd, w, V, k); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
@@ -714,7 +714,7 @@ ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* 
 ttg_status colmajor_to_rows(ttg_op* op, const double* src, int64_t ld_src, double* dst,
                             int64_t ld_dst, int64_t n, int k) {
   dim3 grid((unsigned)((n + 31) / 32), (unsigned)((k + 31) / 32));
-  k_cm_to_rows<<<grid, dim3(32, 8), 0, op->stream>>>(src, ld_src, dst, ld_dst, n, k);
+  k_cm_to_rows<<<grid, dim3(32, 8), 0, op->stream>>>(src, ld_src, dst, ld_dst, n, k); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
@@ -722,26 +722,26 @@ ttg_status colmajor_to_rows(ttg_op* op, const double* src, int64_t ld_src, doubl
 ttg_status rows_to_colmajor(ttg_op* op, const double* src, int64_t ld_src, double* dst,
                             int64_t ld_dst, int64_t n, int k) {
   dim3 grid((unsigned)((n + 31) / 32), (unsigned)((k + 31) / 32));
-  k_rows_to_cm<<<grid, dim3(32, 8), 0, op->stream>>>(src, ld_src, dst, ld_dst, n, k);
+  k_rows_to_cm<<<grid, dim3(32, 8), 0, op->stream>>>(src, ld_src, dst, ld_dst, n, k); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
 
 ttg_status lanczos_step(ttg_op* op, double* v, double* v0, const double* hv, double* ab, int it) {
-  k_lanczos_step<<<1, 1024, 0, op->stream>>>(v, v0, hv, op->n, op->ld, ab, it);
+  k_lanczos_step<<<1, 1024, 0, op->stream>>>(v, v0, hv, op->n, op->ld, ab, it); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
 
 ttg_status normalize(ttg_op* op, double* v) {
-  k_normalize<<<1, 1024, 0, op->stream>>>(v, op->n, op->ld);
+  k_normalize<<<1, 1024, 0, op->stream>>>(v, op->n, op->ld); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
 
 ttg_status fermi(ttg_op* op, const double* eig, int k, double ne, double kT, int max_iter,
                  double* occ, double* out) {
-  k_fermi<<<1, 256, 0, op->stream>>>(eig, k, ne, kT, max_iter, occ, out);
+  k_fermi<<<1, 256, 0, op->stream>>>(eig, k, ne, kT, max_iter, occ, out); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
@@ -820,11 +820,11 @@ extern "C" ttg_status ttg_gram_noalloc(const double* x_dev, const double* y_dev,
   if (nsplit < 1) nsplit = 1;
   const int64_t rows = (n + nsplit - 1) / nsplit;
   ttg::k_gram_tn<<<dim3(tp, tq, (unsigned)nsplit), 256, 0, st>>>(x_dev, y_dev, n, k, ld, rows,
-                                                                scratch);
+                                                                scratch); TTG_COUNT();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return TTG_CUDA_ERR;
   ttg::k_reduce_splits<<<(unsigned)std::min<int64_t>((kk + 255) / 256, 1024), 256, 0, st>>>(
-      scratch, (int)nsplit, kk, s_dev);
+      scratch, (int)nsplit, kk, s_dev); TTG_COUNT();
   e = cudaGetLastError();
   return e == cudaSuccess ? TTG_OK : TTG_CUDA_ERR;
 }

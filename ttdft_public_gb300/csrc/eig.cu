@@ -378,14 +378,14 @@ ttg_status sym_topk(ttg_op* op, double* A, int n, int r, double* w, double* U, i
   double* S = tt + n;
   double* Li = S + (int64_t)r * r;
   double* U2 = Li + (int64_t)r * r;
-  k_symmetrize_lower<<<64, 256, 0, st>>>(A, n);
+  k_symmetrize_lower<<<64, 256, 0, st>>>(A, n); TTG_COUNT();
   TTG_LAUNCHED(op);
   const size_t sm_tr = (size_t)(2 * n + n / kCluster + 1 + kTrThreads) * sizeof(double);
-  k_tridiag_cluster<<<kCluster, kTrThreads, sm_tr, st>>>(A, n, dd, ee, tt, Vr);
+  k_tridiag_cluster<<<kCluster, kTrThreads, sm_tr, st>>>(A, n, dd, ee, tt, Vr); TTG_COUNT();
   TTG_LAUNCHED(op);
-  k_tridiag_multisect<<<r, 32, 2 * n * sizeof(double), st>>>(dd, ee, n, w);
+  k_tridiag_multisect<<<r, 32, 2 * n * sizeof(double), st>>>(dd, ee, n, w); TTG_COUNT();
   TTG_LAUNCHED(op);
-  k_tridiag_vectors<<<r, kVecThreads, 6 * n * sizeof(double), st>>>(dd, ee, tt, Vr, w, n, U);
+  k_tridiag_vectors<<<r, kVecThreads, 6 * n * sizeof(double), st>>>(dd, ee, tt, Vr, w, n, U); TTG_COUNT();
   TTG_LAUNCHED(op);
   // Cholesky QR2: U <- U L^-T with U^T U = L L^T
   for (int pass = 0; pass < 2; ++pass) {
@@ -396,7 +396,7 @@ ttg_status sym_topk(ttg_op* op, double* A, int n, int r, double* w, double* U, i
     TTG_CUDA_TRY(cudaMemcpyAsync(&stat, d_status, 4, cudaMemcpyDeviceToHost, st));
     TTG_CUDA_TRY(cudaStreamSynchronize(st));
     if (stat != 0) {
-      k_cgs2<<<1, 1024, 0, st>>>(U, n, r, S);
+      k_cgs2<<<1, 1024, 0, st>>>(U, n, r, S); TTG_COUNT();
       TTG_LAUNCHED(op);
       TTG_CUDA_TRY(cudaMemsetAsync(d_status, 0, 4, st));
       break;

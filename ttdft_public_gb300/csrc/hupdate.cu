@@ -12,8 +12,8 @@
 // Here the sparsity pattern is the one fixed when the operator was created,
 // and the values are recomputed in place: the Tucker sum is factorised
 // through (x-pair, y-pair) intermediates
-//   T1[xp][b][c]     = sum_a PX_a[xp] G_abc                  (one FP64 GEMM)
-//   T2[yp][xp][c]    = sum_b PY_b[yp] T1[xp][b][c]           (batched FP64 GEMM)
+//   T1[b][xp][c]     = sum_a PX_a[xp] G_abc                  (batched FP64 GEMM)
+//   T2[yp][xp][c]    = sum_b PY_b[yp] T1[b][xp][c]           (one FP64 GEMM)
 //   H_pot[I,J]       = sum_c PZ_c[zp] T2[yp][xp][c]          (per entry, r_c FMAs)
 // and each new value is written straight into every device format through
 // the position maps recorded when the formats were packed.  FP64 throughout.
@@ -172,12 +172,12 @@ ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const d
   TTG_CUDA_TRY(cudaMemcpyAsync(w + off_y, hy.data(), hy.size() * 8, cudaMemcpyHostToDevice, st));
   TTG_CUDA_TRY(cudaMemcpyAsync(w + off_z, hz.data(), hz.size() * 8, cudaMemcpyHostToDevice, st));
   TTG_CUDA_TRY(cudaMemcpyAsync(w + off_g, G, ncore * 8, cudaMemcpyHostToDevice, st));
-  // T1[xp][(b,c)] = sum_a PXp[xp][a] G[a + ra (b + rb c)]
-  TTG_TRY(dgemm(st, (int)nxp, rb * rc, ra, 1, DOp{w + off_x, ra, 1, 0}, DOp{w + off_g, 1, ra, 0},
-                w + off_t1, (int64_t)rb * rc, 1, 0, P.work2));
-  // T2[yp][xp][c] = sum_b PYp[yp][b] T1[xp][b + rb c]   (batch over xp)
-  TTG_TRY(dgemm(st, (int)nyp, rc, rb, (int)nxp, DOp{w + off_y, rb, 1, 0},
-                DOp{w + off_t1, 1, rb, (int64_t)rb * rc}, w + off_t2, nxp * rc, 1, rc, P.work2));
+  // T1[b][xp][c] = sum_a PXp[xp][a] G[a + ra (b + rb c)]   (batch over b)
+  TTG_TRY(dgemm(st, (int)nxp, rc, ra, rb, DOp{w + off_x, ra, 1, 0},
+                DOp{w + off_g, 1, (int64_t)ra * rb, ra}, w + off_t1, rc, 1, nxp * rc, P.work2));
+  // T2[yp][(xp, c)] = sum_b PYp[yp][b] T1[b][(xp, c)]: one GEMM, N = nxp * rc
+  TTG_TRY(dgemm(st, (int)nyp, (int)(nxp * rc), rb, 1, DOp{w + off_y, rb, 1, 0},
+                DOp{w + off_t1, nxp * rc, 1, 0}, w + off_t2, nxp * rc, 1, 0, P.work2));
   UpdateArgs a{};
   a.row_ptr = P.row_ptr.as<int64_t>();
   a.col = P.col.as<int>();
@@ -201,7 +201,7 @@ ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const d
   a.t16 = op->tiles.v16.as<__nv_bfloat16>();
   a.n = op->n;
   const int wpb = 8;
-  k_update_values<<<(unsigned)((op->n + wpb - 1) / wpb), 32 * wpb, 0, st>>>(a);
+  k_update_values<<<(unsigned)((op->n + wpb - 1) / wpb), 32 * wpb, 0, st>>>(a); TTG_COUNT();
   TTG_LAUNCHED(op);
   TTG_CUDA_TRY(cudaStreamSynchronize(st));
   return TTG_OK;

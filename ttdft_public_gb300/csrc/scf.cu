@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "ttg_internal.cuh"
@@ -35,19 +36,30 @@ namespace ttg {
 namespace {
 
 constexpr int DM = 64, DN = 64, DK = 16;
+constexpr int64_t kNumSMs = 152;
 
 // C[z] (+)= A[z] B[z] over a K range; split s of z_total = batch*splits writes
 // its partial to part + s*... when part != nullptr.
+// sym: the product is symmetric (a Gram matrix); tiles strictly above the
+// diagonal are skipped and filled by k_mirror_upper afterwards.
 __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, int splits, DOp A, DOp B,
                                                double* C, int64_t c_rs, int64_t c_cs, int64_t c_bs,
-                                               double* part) {
+                                               double* part, int sym) {
   __shared__ double sA[DK][DM + 1];
   __shared__ double sB[DK][DN + 1];
   const int zz = blockIdx.z;
   const int z = zz / splits, sp = zz % splits;
   const int kchunk = (K + splits - 1) / splits;
   const int kbeg = sp * kchunk, kend = min(K, kbeg + kchunk);
-  const int m0 = blockIdx.y * DM, n0 = blockIdx.x * DN;
+  int mt = blockIdx.y, nt = blockIdx.x;
+  if (sym) {          // blockIdx.x enumerates the tiles on and below the diagonal
+    const int i = blockIdx.x;
+    mt = (int)((sqrt(8.0 * i + 1.0) - 1.0) * 0.5);
+    while ((mt + 1) * (mt + 2) / 2 <= i) ++mt;
+    while (mt * (mt + 1) / 2 > i) --mt;
+    nt = i - mt * (mt + 1) / 2;
+  }
+  const int m0 = mt * DM, n0 = nt * DN;
   const double* Ab = A.p + (int64_t)z * A.bs;
   const double* Bb = B.p + (int64_t)z * B.bs;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -92,16 +104,28 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, int splits, 
 }
 
 __global__ void k_dgemm_reduce(const double* __restrict__ part, int batch, int splits, int M,
-                               int N, double* C, int64_t c_rs, int64_t c_cs, int64_t c_bs) {
+                               int N, double* C, int64_t c_rs, int64_t c_cs, int64_t c_bs,
+                               int sym) {
   const int64_t total = (int64_t)batch * M * N;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int z = (int)(e / ((int64_t)M * N));
     const int64_t r = e - (int64_t)z * M * N;
     const int m = (int)(r / N), n = (int)(r - (int64_t)m * N);
+    if (sym && n > m) continue;
     double s = 0.0;
     for (int sp = 0; sp < splits; ++sp) s += part[(((int64_t)z * splits + sp) * M + m) * N + n];
     C[(int64_t)z * c_bs + (int64_t)m * c_rs + (int64_t)n * c_cs] = s;
+  }
+}
+
+// C[m, n] = C[n, m] for n > m (square, batch 1).
+__global__ void k_mirror_upper(double* C, int M, int64_t c_rs, int64_t c_cs) {
+  const int64_t total = (int64_t)M * M;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(e / M), n = (int)(e - (int64_t)m * M);
+    if (n > m) C[(int64_t)m * c_rs + (int64_t)n * c_cs] = C[(int64_t)n * c_rs + (int64_t)m * c_cs];
   }
 }
 
@@ -125,16 +149,20 @@ int gblocks(int64_t n) {
 
 // Generic FP64 GEMM with automatic split-K when the output is small.
 ttg_status dgemm(cudaStream_t st, int M, int N, int K, int batch, DOp A, DOp B, double* C,
-                 int64_t c_rs, int64_t c_cs, int64_t c_bs, DevBuf& scratch) {
+                 int64_t c_rs, int64_t c_cs, int64_t c_bs, DevBuf& scratch, bool sym) {
   if (M <= 0 || N <= 0 || batch <= 0) return TTG_OK;
-  const int64_t tiles = (int64_t)((M + DM - 1) / DM) * ((N + DN - 1) / DN) * batch;
+  if (sym && (M != N || batch != 1)) return TTG_BAD_ARG;
+  const int64_t tm = (M + DM - 1) / DM, tn = (N + DN - 1) / DN;
+  const int64_t tiles = sym ? tm * (tm + 1) / 2 : tm * tn * batch;
+  // split K so that the CTAs fill the SMs evenly (FP64 throughput is per
+  // SM: the busiest SM sets the time)
   int splits = 1;
-  if (tiles < 2 * 152 && K > 4 * DK) {
-    splits = (int)std::min<int64_t>((2 * 152 + tiles - 1) / tiles, (K + 4 * DK - 1) / (4 * DK));
+  if (tiles < kNumSMs && K > 4 * DK) {
+    splits = (int)std::min<int64_t>(kNumSMs / tiles, (K + 4 * DK - 1) / (4 * DK));
     splits = std::max(1, std::min(splits, 256));
   }
   if ((int64_t)batch * splits > 65535) return TTG_BAD_ARG;
-  dim3 grid((N + DN - 1) / DN, (M + DM - 1) / DM, batch * splits);
+  dim3 grid(sym ? (unsigned)tiles : (unsigned)tn, sym ? 1u : (unsigned)tm, batch * splits);
   if (grid.y > 65535) return TTG_BAD_ARG;
   double* part = nullptr;
   if (splits > 1) {
@@ -142,11 +170,15 @@ ttg_status dgemm(cudaStream_t st, int M, int N, int K, int batch, DOp A, DOp B, 
     if (scratch.bytes < need) TTG_TRY(scratch.alloc(need));
     part = scratch.as<double>();
   }
-  k_dgemm<<<grid, 256, 0, st>>>(M, N, K, splits, A, B, C, c_rs, c_cs, c_bs, part);
+  k_dgemm<<<grid, 256, 0, st>>>(M, N, K, splits, A, B, C, c_rs, c_cs, c_bs, part, sym ? 1 : 0); TTG_COUNT();
   if (cudaGetLastError() != cudaSuccess) return TTG_CUDA_ERR;
   if (splits > 1) {
     k_dgemm_reduce<<<gblocks((int64_t)batch * M * N), 256, 0, st>>>(part, batch, splits, M, N, C,
-                                                                     c_rs, c_cs, c_bs);
+                                                                     c_rs, c_cs, c_bs, sym ? 1 : 0); TTG_COUNT();
+    if (cudaGetLastError() != cudaSuccess) return TTG_CUDA_ERR;
+  }
+  if (sym) {
+    k_mirror_upper<<<gblocks((int64_t)M * M), 256, 0, st>>>(C, M, c_rs, c_cs); TTG_COUNT();
     if (cudaGetLastError() != cudaSuccess) return TTG_CUDA_ERR;
   }
   return TTG_OK;
@@ -180,16 +212,16 @@ ttg_status mode_gram(cudaStream_t st, const double* T, const int* n, int d, doub
   const int64_t n0 = n[0], n1 = n[1], n2 = n[2];
   if (d == 0)
     return dgemm(st, (int)n0, (int)n0, (int)(n1 * n2), 1, DOp{T, 1, n0, 0}, DOp{T, n0, 1, 0}, G,
-                 1, n0, 0, scratch);
+                 1, n0, 0, scratch, true);
   if (d == 2)
     return dgemm(st, (int)n2, (int)n2, (int)(n0 * n1), 1, DOp{T, n0 * n1, 1, 0},
-                 DOp{T, 1, n0 * n1, 0}, G, 1, n2, 0, scratch);
+                 DOp{T, 1, n0 * n1, 0}, G, 1, n2, 0, scratch, true);
   // mode 1: sum over slabs l of T_l^T T_l (n1 x n1), T_l = (n0 x n1) column-major
   const size_t need = (size_t)n2 * n1 * n1 * sizeof(double);
   if (scratch2.bytes < need) TTG_TRY(scratch2.alloc(need));
   TTG_TRY(dgemm(st, (int)n1, (int)n1, (int)n0, (int)n2, DOp{T, n0, 1, n0 * n1},
                 DOp{T, 1, n0, n0 * n1}, scratch2.as<double>(), 1, n1, n1 * n1, scratch));
-  k_sum_batches<<<gblocks(n1 * n1), 256, 0, st>>>(scratch2.as<double>(), (int)n2, n1 * n1, G);
+  k_sum_batches<<<gblocks(n1 * n1), 256, 0, st>>>(scratch2.as<double>(), (int)n2, n1 * n1, G); TTG_COUNT();
   return cudaGetLastError() == cudaSuccess ? TTG_OK : TTG_CUDA_ERR;
 }
 
@@ -331,6 +363,53 @@ __global__ void k_gauss_apply(const double* __restrict__ alpha, const double* __
   }
 }
 
+// Slab c' of term t of the Hartree energy:
+//   part[t][c'] = sum_{a',b'} G[a',b',c'] (Kx_t Hs Ky_t)[a',b'],
+//   Hs[a,b] = sum_c G[a,b,c] Kz_t[c,c'].
+// K_d (r_d x r_d per term, column-major, symmetric) in global memory; Hs and
+// Kx Hs in dynamic shared memory (2 r0 r1 doubles).
+__global__ void __launch_bounds__(256) k_hartree_energy_slab(
+    const double* __restrict__ G, int r0, int r1, int r2, const double* __restrict__ Kx,
+    const double* __restrict__ Ky, const double* __restrict__ Kz, double* __restrict__ part) {
+  extern __shared__ double hsm[];
+  double* Hs = hsm;
+  double* Tm = hsm + r0 * r1;
+  __shared__ double red[32];
+  const int cp = blockIdx.x, t = blockIdx.y;
+  const double* kx = Kx + (int64_t)t * r0 * r0;
+  const double* ky = Ky + (int64_t)t * r1 * r1;
+  const double* kz = Kz + (int64_t)t * r2 * r2 + (int64_t)cp * r2;   // column c'
+  const int nab = r0 * r1;
+  for (int e = threadIdx.x; e < nab; e += blockDim.x) {
+    double acc = 0.0;
+    for (int c = 0; c < r2; ++c) acc = fma(G[e + (int64_t)nab * c], kz[c], acc);
+    Hs[e] = acc;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nab; e += blockDim.x) {
+    const int ap = e % r0, b = e / r0;
+    double acc = 0.0;
+    for (int a = 0; a < r0; ++a) acc = fma(kx[ap + (int64_t)a * r0], Hs[a + r0 * b], acc);
+    Tm[e] = acc;
+  }
+  __syncthreads();
+  double sum = 0.0;
+  for (int e = threadIdx.x; e < nab; e += blockDim.x) {
+    const int ap = e % r0, bp = e / r0;
+    double acc = 0.0;
+    for (int b = 0; b < r1; ++b) acc = fma(Tm[ap + r0 * b], ky[b + (int64_t)bp * r1], acc);
+    sum = fma(G[e + (int64_t)nab * cp], acc, sum);
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    part[(int64_t)t * r2 + cp] = tot;
+  }
+}
+
 __global__ void k_dot(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
                       double* out) {
   __shared__ double red[32];
@@ -409,9 +488,13 @@ ttg_status ttg_tucker_sthosvd(ttg_op* op, const double* t_dev, const int32_t* di
     if (n[d] <= 0 || n[d] > 2048) return TTG_BAD_ARG;
   cudaStream_t st = op->stream;
   const int64_t total = (int64_t)n[0] * n[1] * n[2];
-  DevBuf A, B, gram, part, part2, norm;
-  TTG_TRY(A.alloc(total * 8));
-  TTG_TRY(B.alloc(total * 8));
+  DevBuf norm;
+  DevBuf& A = op->sth_a;
+  DevBuf& B = op->sth_b;
+  DevBuf& part = op->sth_part;
+  DevBuf& part2 = op->sth_part2;
+  if (A.bytes < (size_t)total * 8) TTG_TRY(A.alloc(total * 8));
+  if (B.bytes < (size_t)total * 8) TTG_TRY(B.alloc(total * 8));
   TTG_TRY(norm.alloc(4096 * 8));
   TTG_CUDA_TRY(cudaMemcpyAsync(A.p, t_dev, total * 8, cudaMemcpyDeviceToDevice, st));
   // ||T||^2 for the truncation threshold eps^2 ||T||^2 / 3 per mode
@@ -422,8 +505,8 @@ ttg_status ttg_tucker_sthosvd(ttg_op* op, const double* t_dev, const int32_t* di
     TTG_CUDA_TRY(cudaMemcpyAsync(w1.p, ones.data(), 4096 * 8, cudaMemcpyHostToDevice, st));
     const int nb = 1024;
     k_wsum<<<nb, 256, 0, st>>>(A.as<double>(), A.as<double>(), w1.as<double>(), w1.as<double>(),
-                               w1.as<double>(), n[0], n[1], n[2], norm.as<double>());
-    k_sum_partials<<<1, 32, 0, st>>>(norm.as<double>(), nb, norm.as<double>() + 2048);
+                               w1.as<double>(), n[0], n[1], n[2], norm.as<double>()); TTG_COUNT();
+    k_sum_partials<<<1, 32, 0, st>>>(norm.as<double>(), nb, norm.as<double>() + 2048); TTG_COUNT();
     TTG_LAUNCHED(op);
     TTG_CUDA_TRY(cudaStreamSynchronize(st));
   }
@@ -439,7 +522,7 @@ ttg_status ttg_tucker_sthosvd(ttg_op* op, const double* t_dev, const int32_t* di
     if (op->kk0.bytes < kk) TTG_TRY(op->kk0.alloc(kk));
     TTG_TRY(mode_gram(st, A.as<double>(), cur, d, op->kk0.as<double>(), part, part2));
     // trace of the Gram = sum of all eigenvalues
-    k_diag_sum<<<1, 256, 0, st>>>(op->kk0.as<double>(), nd, norm.as<double>() + 2049);
+    k_diag_sum<<<1, 256, 0, st>>>(op->kk0.as<double>(), nd, norm.as<double>() + 2049); TTG_COUNT();
     TTG_LAUNCHED(op);
     // the rcap largest eigenpairs in FP64 (the truncation needs eigenvectors whose
     // eigenvalues are many orders below the largest one)
@@ -553,34 +636,37 @@ ttg_status ttg_hartree_energy(int32_t K, const double* alpha, const double* omeg
     TTG_CUDA_TRY(cudaMemcpyAsync(x[d].p, xs[d], q * 8, cudaMemcpyHostToDevice, S.s));
     TTG_CUDA_TRY(cudaMemcpyAsync(wu[d].p, h.data(), h.size() * 8, cudaMemcpyHostToDevice, S.s));
     k_gauss_apply<<<dim3(q, K), 128, q * 8, S.s>>>(dalpha.as<double>(), x[d].as<double>(), q,
-                                                    wu[d].as<double>(), r[d], M[d].as<double>());
+                                                    wu[d].as<double>(), r[d], M[d].as<double>()); TTG_COUNT();
     TTG_CUDA_TRY(cudaGetLastError());
     // K_t[a, a'] = sum_q WU[q, a] M_t[q, a']  (batched over t), column-major r x r
     TTG_TRY(dgemm(S.s, r[d], r[d], q, K, DOp{wu[d].as<double>(), q, 1, 0},
                   DOp{M[d].as<double>(), 1, q, (int64_t)r[d] * q}, Kd[d].as<double>(), 1, r[d],
                   (int64_t)r[d] * r[d], scratch));
   }
-  TTG_TRY(t0.alloc(ncore * 8));
-  TTG_TRY(t1.alloc(ncore * 8));
-  TTG_TRY(res.alloc((size_t)K * 8));
-  int cur[3] = {r[0], r[1], r[2]};
-  for (int t = 0; t < K; ++t) {
-    // T = G x1 Kx_t x2 Ky_t x3 Kz_t (K_t symmetric), then E_t = <G, T>
-    const double* in = core.as<double>();
-    double* bufs[2] = {t0.as<double>(), t1.as<double>()};
-    for (int d = 0; d < 3; ++d) {
-      TTG_TRY(mode_product(S.s, in, cur, d, Kd[d].as<double>() + (int64_t)t * r[d] * r[d], r[d],
-                           bufs[d & 1], scratch));
-      in = bufs[d & 1];
-    }
-    k_dot<<<1, 256, 0, S.s>>>(core.as<double>(), in, ncore, res.as<double>() + t);
-    TTG_CUDA_TRY(cudaGetLastError());
-  }
-  std::vector<double> e(K);
-  TTG_CUDA_TRY(cudaMemcpyAsync(e.data(), res.p, K * 8, cudaMemcpyDeviceToHost, S.s));
+  // E_t = <G, G x1 Kx_t x2 Ky_t x3 Kz_t>, one CTA per (slab c', term t)
+  TTG_TRY(res.alloc((size_t)K * r[2] * 8));
+  const size_t smem = (size_t)2 * r[0] * r[1] * sizeof(double);
+  if (smem > 200 * 1024) return TTG_BAD_ARG;
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(k_hartree_energy_slab,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  });
+  if (attr_err != cudaSuccess) return TTG_CUDA_ERR;
+  k_hartree_energy_slab<<<dim3(r[2], K), 256, smem, S.s>>>(
+      core.as<double>(), r[0], r[1], r[2], Kd[0].as<double>(), Kd[1].as<double>(),
+      Kd[2].as<double>(), res.as<double>()); TTG_COUNT();
+  TTG_CUDA_TRY(cudaGetLastError());
+  std::vector<double> e((size_t)K * r[2]);
+  TTG_CUDA_TRY(cudaMemcpyAsync(e.data(), res.p, e.size() * 8, cudaMemcpyDeviceToHost, S.s));
   TTG_CUDA_TRY(cudaStreamSynchronize(S.s));
   double s = 0.0;
-  for (int t = 0; t < K; ++t) s += omega[t] * e[t];
+  for (int t = 0; t < K; ++t) {
+    double et = 0.0;
+    for (int c = 0; c < r[2]; ++c) et += e[(size_t)t * r[2] + c];
+    s += omega[t] * et;
+  }
   *energy = 0.5 * s;
   return TTG_OK;
 }
@@ -589,7 +675,7 @@ ttg_status ttg_grid_lda(const double* rho_dev, int64_t n, double* v_dev, double*
                         int32_t accumulate_v, void* stream) {
   if (!rho_dev || n <= 0) return TTG_BAD_ARG;
   Stream S(stream);
-  k_lda<<<gblocks(n), 256, 0, S.s>>>(rho_dev, n, v_dev, e_dev, accumulate_v);
+  k_lda<<<gblocks(n), 256, 0, S.s>>>(rho_dev, n, v_dev, e_dev, accumulate_v); TTG_COUNT();
   TTG_CUDA_TRY(cudaGetLastError());
   return TTG_OK;
 }
@@ -603,8 +689,8 @@ ttg_status ttg_grid_integrate(const double* f_dev, const double* g_dev, const in
   const int nb = 1024;
   TTG_TRY(part.alloc((nb + 1) * 8));
   k_wsum<<<nb, 256, 0, S.s>>>(f_dev, g_dev, wx_dev, wy_dev, wz_dev, dims[0], dims[1], dims[2],
-                              part.as<double>());
-  k_sum_partials<<<1, 32, 0, S.s>>>(part.as<double>(), nb, part.as<double>() + nb);
+                              part.as<double>()); TTG_COUNT();
+  k_sum_partials<<<1, 32, 0, S.s>>>(part.as<double>(), nb, part.as<double>() + nb); TTG_COUNT();
   TTG_CUDA_TRY(cudaGetLastError());
   TTG_CUDA_TRY(cudaMemcpyAsync(result, part.as<double>() + nb, 8, cudaMemcpyDeviceToHost, S.s));
   TTG_CUDA_TRY(cudaStreamSynchronize(S.s));
@@ -619,7 +705,7 @@ ttg_status ttg_grid_cp_sum(int32_t nterms, const double* coef_dev, const double*
   Stream S(stream);
   const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
   k_cp_sum<<<gblocks(n), 256, 0, S.s>>>(nterms, coef_dev, fx_dev, fy_dev, fz_dev, dims[0], dims[1],
-                                        dims[2], out_dev, accumulate);
+                                        dims[2], out_dev, accumulate); TTG_COUNT();
   TTG_CUDA_TRY(cudaGetLastError());
   return TTG_OK;
 }
@@ -633,7 +719,7 @@ ttg_status ttg_grid_ion_potential(int32_t natoms, const double* pos_dev, const d
   Stream S(stream);
   const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
   k_ion_potential<<<gblocks(n), 256, 0, S.s>>>(natoms, pos_dev, z_dev, width, gx_dev, gy_dev, gz_dev,
-                                               dims[0], dims[1], dims[2], out_dev);
+                                               dims[0], dims[1], dims[2], out_dev); TTG_COUNT();
   TTG_CUDA_TRY(cudaGetLastError());
   return TTG_OK;
 }
@@ -647,7 +733,7 @@ ttg_status ttg_grid_lincomb(int32_t nterms, const double* const* fields_dev, con
     t.f[m] = fields_dev[m];
     t.c[m] = coef[m];
   }
-  k_lincomb<<<gblocks(n), 256, 0, S.s>>>(t, nterms, n, out_dev, take_abs);
+  k_lincomb<<<gblocks(n), 256, 0, S.s>>>(t, nterms, n, out_dev, take_abs); TTG_COUNT();
   TTG_CUDA_TRY(cudaGetLastError());
   return TTG_OK;
 }

@@ -652,18 +652,18 @@ static ttg_status rg_values(ttg_op* op, int prec, void** out) {
   const int grid = grid_for(cnt, 256);
   if (prec == TTG_PREC_FP32 && !rg.v32.p) {
     TTG_TRY(rg.v32.alloc(cnt * sizeof(float)));
-    k_convert_vals<float><<<grid, 256, 0, op->stream>>>(rg.v64.as<double>(), rg.v32.as<float>(), cnt);
+    k_convert_vals<float><<<grid, 256, 0, op->stream>>>(rg.v64.as<double>(), rg.v32.as<float>(), cnt); TTG_COUNT();
     TTG_LAUNCHED(op);
     op->device_bytes += rg.v32.bytes;
   } else if (prec == TTG_PREC_BF16 && !rg.v16.p) {
     TTG_TRY(rg.v16.alloc(cnt * sizeof(__nv_bfloat16)));
     k_convert_vals<__nv_bfloat16><<<grid, 256, 0, op->stream>>>(rg.v64.as<double>(),
-                                                               rg.v16.as<__nv_bfloat16>(), cnt);
+                                                               rg.v16.as<__nv_bfloat16>(), cnt); TTG_COUNT();
     TTG_LAUNCHED(op);
     op->device_bytes += rg.v16.bytes;
   } else if (prec == TTG_PREC_DF64 && !rg.vdf.p) {
     TTG_TRY(rg.vdf.alloc(cnt * sizeof(float2)));
-    k_split_vals<<<grid, 256, 0, op->stream>>>(rg.v64.as<double>(), rg.vdf.as<float2>(), cnt);
+    k_split_vals<<<grid, 256, 0, op->stream>>>(rg.v64.as<double>(), rg.vdf.as<float2>(), cnt); TTG_COUNT();
     TTG_LAUNCHED(op);
     op->device_bytes += rg.vdf.bytes;
   }
@@ -684,7 +684,7 @@ static ttg_status launch_step_t(ttg_op* op, const TV* vals, const void* src, con
   k_cheb_step<TV, TS, TA, G, VEC, CH><<<(unsigned)op->rg.n_groups, threads, 0, op->stream>>>(
       op->rg.gptr.as<int64_t>(), op->rg.gcol.as<int>(), vals,
       reinterpret_cast<const TS*>(src), reinterpret_cast<const TS*>(xold),
-      reinterpret_cast<TS*>(dst), op->n, k, op->ld, (TA)alpha, (TA)beta, (TA)delta);
+      reinterpret_cast<TS*>(dst), op->n, k, op->ld, (TA)alpha, (TA)beta, (TA)delta); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
@@ -702,7 +702,7 @@ ttg_status launch_cheb_step(ttg_op* op, int prec, const void* src, const void* x
       k_spmv_rg<kGroupRows><<<blocks, 32 * wpb, 0, op->stream>>>(
           op->rg.gptr.as<int64_t>(), op->rg.gcol.as<int>(), op->rg.v64.as<double>(),
           reinterpret_cast<const double*>(src), reinterpret_cast<double*>(dst), op->n,
-          op->rg.n_groups, op->ld, alpha, beta);
+          op->rg.n_groups, op->ld, alpha, beta); TTG_COUNT();
       TTG_LAUNCHED(op);
       return TTG_OK;
     }
@@ -749,14 +749,14 @@ ttg_status launch_apply_df64(ttg_op* op, const double* src, double* dst, int k) 
   TTG_TRY(rg_values(op, TTG_PREC_DF64, &vdf));
   const int64_t rows = op->n + op->nproj;
   k_split_df64<<<grid_for(rows * k, 256), 256, 0, op->stream>>>(src, op->wdf.as<float2>(), rows,
-                                                                k, op->ld);
+                                                                k, op->ld); TTG_COUNT();
   TTG_LAUNCHED(op);
   if (op->rg.n_groups == 0) return TTG_OK;
   const int threads = std::min(512, (k + 31) / 32 * 32);
   dim3 grid((unsigned)op->rg.n_groups, (unsigned)((k + threads - 1) / threads));
   k_apply_df64<kGroupRows><<<grid, threads, 0, op->stream>>>(
       op->rg.gptr.as<int64_t>(), op->rg.gcol.as<int>(), op->rg.vdf.as<float2>(),
-      op->wdf.as<float2>(), dst, op->n, k, op->ld);
+      op->wdf.as<float2>(), dst, op->n, k, op->ld); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
@@ -773,10 +773,10 @@ static ttg_status proj_w_t(ttg_op* op, TS* src, int k) {
   const int threads = std::min(256, (k + 31) / 32 * 32);
   k_proj_partial<TS, TA><<<dim3(op->nproj, nsplit), threads, 0, op->stream>>>(
       op->C.ptr.as<int64_t>(), op->C.col.as<int>(), op->C.val.as<double>(), src, k, op->ld,
-      op->wpart.as<TA>(), nsplit);
+      op->wpart.as<TA>(), nsplit); TTG_COUNT();
   TTG_LAUNCHED(op);
   k_proj_reduce<TS, TA><<<op->nproj, threads, 0, op->stream>>>(op->wpart.as<TA>(), nsplit, src,
-                                                              op->n, k, op->ld);
+                                                              op->n, k, op->ld); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
@@ -808,6 +808,7 @@ ttg_status launch_convert(ttg_op* op, int from, int to, const void* src, void* d
         (const __nv_bfloat16*)src, (double*)dst, rows, k, op->ld);
   else
     return TTG_BAD_ARG;
+  TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }

@@ -421,7 +421,7 @@ static ttg_status launch_tc_t(ttg_op* op, const void* hval, const void* src, con
       op->tiles.tptr.as<int64_t>(), op->tiles.tcol.as<int>(), op->tiles.rowmap.as<int>(),
       reinterpret_cast<const typename TcTraits<T>::HV*>(hval), reinterpret_cast<const T*>(src),
       reinterpret_cast<const T*>(xold), reinterpret_cast<T*>(dst), k, op->ld, (float)alpha,
-      (float)beta, (float)delta);
+      (float)beta, (float)delta); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }

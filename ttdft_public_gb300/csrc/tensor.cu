@@ -263,7 +263,7 @@ ttg_status gemm(cudaStream_t st, int M, int N, int K, int batch, Operand A, Oper
   if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return TTG_OK;
   dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
   if (grid.y > 65535 || grid.z > 65535) return TTG_BAD_ARG;
-  k_gemm_x3<EPI><<<grid, NTHR, 0, st>>>(M, N, K, A, B, C, c_rs, c_cs, c_bs, alpha, beta, sq);
+  k_gemm_x3<EPI><<<grid, NTHR, 0, st>>>(M, N, K, A, B, C, c_rs, c_cs, c_bs, alpha, beta, sq); TTG_COUNT();
   if (launches) (*launches)++;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TTG_OK : TTG_CUDA_ERR;
@@ -313,7 +313,7 @@ ttg_status ttg_density(ttg_op* op, const ttg_block* X, const double* occ_host, i
   double* stage = sc.get<double>(std::max<int64_t>({(int64_t)nx * rx, (int64_t)ny * ry,
                                                     (int64_t)nz * rz, (int64_t)nx * ny * nz}));
   if (!Xf || !Ux || !Uy || !Uz || !w || !P1 || !P2 || !rho || !stage) return TTG_OOM;
-  k_block_to_f32<<<blocks_for(n * S), 256, 0, st>>>(X->x.as<double>(), n, k, op->ld, Xf, S);
+  k_block_to_f32<<<blocks_for(n * S), 256, 0, st>>>(X->x.as<double>(), n, k, op->ld, Xf, S); TTG_COUNT();
   TTG_LAUNCHED(op);
   // basis values at the nodes, column-major (nodes x rank)
   const double* hs[3] = {ux, uy, uz};
@@ -321,7 +321,7 @@ ttg_status ttg_density(ttg_op* op, const ttg_block* X, const double* occ_host, i
   const int64_t cnt[3] = {(int64_t)nx * rx, (int64_t)ny * ry, (int64_t)nz * rz};
   for (int d = 0; d < 3; ++d) {
     TTG_CUDA_TRY(cudaMemcpyAsync(stage, hs[d], cnt[d] * 8, cudaMemcpyHostToDevice, st));
-    k_d2f<<<blocks_for(cnt[d]), 256, 0, st>>>(stage, ds[d], cnt[d]);
+    k_d2f<<<blocks_for(cnt[d]), 256, 0, st>>>(stage, ds[d], cnt[d]); TTG_COUNT();
     TTG_LAUNCHED(op);
   }
   std::vector<float> wh(S, 0.f);
@@ -345,7 +345,7 @@ ttg_status ttg_density(ttg_op* op, const ttg_block* X, const double* occ_host, i
                           Operand{P2, (int64_t)ny * nx * S, 1, 0}, nullptr, 0, 0, 0, 1.f, 0.f,
                           sq, &op->launches));
   const int64_t ng = (int64_t)nx * ny * nz;
-  k_f2d<<<blocks_for(ng), 256, 0, st>>>(rho, stage, ng);
+  k_f2d<<<blocks_for(ng), 256, 0, st>>>(rho, stage, ng); TTG_COUNT();
   TTG_LAUNCHED(op);
   TTG_CUDA_TRY(cudaMemcpyAsync(rho_host, stage, ng * 8, cudaMemcpyDeviceToHost, st));
   TTG_CUDA_TRY(cudaStreamSynchronize(st));
@@ -396,7 +396,7 @@ ttg_status ttg_hartree(int32_t K, const double* alpha, const double* omega, int3
     TTG_CUDA_TRY(cudaMemcpyAsync(dx, hx[d], ng[d] * 8, cudaMemcpyHostToDevice, st));
     // the z factor carries the term weight: B_big[(t,c), l] = w_t Fz_t[l, c]
     k_expansion_factor<<<dim3(1, ng[d], K), 128, nq[d] * 8, st>>>(
-        d_alpha, K, dx, ng[d], dq, dw, nq[d], du, rr[d], F[d], d == 2 ? d_omega : nullptr);
+        d_alpha, K, dx, ng[d], dq, dw, nq[d], du, rr[d], F[d], d == 2 ? d_omega : nullptr); TTG_COUNT();
     if (cudaGetLastError() != cudaSuccess) return TTG_CUDA_ERR;
   }
   const int64_t ncore = (int64_t)rx * ry * rz;
@@ -409,7 +409,7 @@ ttg_status ttg_hartree(int32_t K, const double* alpha, const double* omega, int3
   double* Vd = sc.get<double>(nout);
   if (!dG || !Gf || !P || !Q || !V || !Vd) return TTG_OOM;
   TTG_CUDA_TRY(cudaMemcpyAsync(dG, G, ncore * 8, cudaMemcpyHostToDevice, st));
-  k_d2f<<<blocks_for(ncore), 256, 0, st>>>(dG, Gf, ncore);
+  k_d2f<<<blocks_for(ncore), 256, 0, st>>>(dG, Gf, ncore); TTG_COUNT();
   SqSum none{nullptr, nullptr, 1, 0, 0};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -442,7 +442,7 @@ ttg_status ttg_hartree(int32_t K, const double* alpha, const double* omega, int3
                           Operand{Bz, 1, (int64_t)K * rz, 0}, V, 1, (int64_t)nx * ny, 0, 1.f, 0.f,
                           none, nullptr));
   cudaEventRecord(e1, st);
-  k_f2d<<<blocks_for(nout), 256, 0, st>>>(V, Vd, nout);
+  k_f2d<<<blocks_for(nout), 256, 0, st>>>(V, Vd, nout); TTG_COUNT();
   TTG_CUDA_TRY(cudaMemcpyAsync(v_host, Vd, nout * 8, cudaMemcpyDeviceToHost, st));
   TTG_CUDA_TRY(cudaStreamSynchronize(st));
   if (kernel_ms) cudaEventElapsedTime(kernel_ms, e0, e1);

@@ -7,6 +7,8 @@
 #include <cstdio>
 #include <vector>
 
+#include <atomic>
+
 #include "ttg.h"
 
 #define TTG_CUDA_TRY(call)                                                  \
@@ -25,6 +27,10 @@
     if (s_ != TTG_OK) return s_;      \
   } while (0)
 
+// Every kernel launch of the library bumps one process-wide counter
+// (ttg_kernel_launches); TTG_LAUNCHED also counts per operator.
+#define TTG_COUNT() (::ttg::g_kernel_launches.fetch_add(1, std::memory_order_relaxed))
+
 // Checks the last launch; counts it.
 #define TTG_LAUNCHED(op)                                                    \
   do {                                                                      \
@@ -38,6 +44,7 @@
   } while (0)
 
 namespace ttg {
+extern std::atomic<long long> g_kernel_launches;
 
 constexpr int kGroupRows = 8;       // rows per row group of the SpMM format
 constexpr int kMaxSlots = 16;
@@ -49,9 +56,25 @@ constexpr int64_t kScalEig = 2048;       // eigenvalues (k)
 constexpr int64_t kScalJacobi = 2048 + 4096;  // unsorted eigenvalues (k)
 
 // Device buffer owned by the library.
+// Owning device allocation: freed by release() or when it goes out of scope.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      bytes = o.bytes;
+      o.p = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
   ttg_status alloc(size_t n);
   void release();
   template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
@@ -140,6 +163,7 @@ struct ttg_op {
   ttg::DevBuf eigbuf;         // eigensolver refinement (5 k*k doubles)
   ttg::DevBuf eigf;           // FP32 tridiagonalisation scratch
   ttg::DevBuf partial;        // split-K partials for the Gram
+  ttg::DevBuf sth_a, sth_b, sth_part, sth_part2;  // STHOSVD work (grow-only)
   ttg::DevBuf scal;           // small FP64 scratch (reductions, status)
   ttg::DevBuf status;         // int32 device status words
   cudaEvent_t ev[ttg::kMaxSlots] = {};
@@ -180,7 +204,7 @@ struct DOp {
   int64_t rs, cs, bs;   // element strides: row (m or k), column (k or n), batch
 };
 ttg_status dgemm(cudaStream_t st, int M, int N, int K, int batch, DOp A, DOp B, double* C,
-                 int64_t c_rs, int64_t c_cs, int64_t c_bs, DevBuf& scratch);
+                 int64_t c_rs, int64_t c_cs, int64_t c_bs, DevBuf& scratch, bool sym = false);
 
 // dense.cu
 ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* S);

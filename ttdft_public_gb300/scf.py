@@ -136,6 +136,16 @@ class Scf:
         self.e_nn = repulsive_energy(sysm.atoms, spec.z_val)
         self.timings = {}
 
+    def close(self):
+        """Releases the operator and the device fields of this run."""
+        if getattr(self, "op", None) is not None:
+            self.op.close()
+            self.op = None
+        for name in ("X", "rho", "vloc", "wq", "rho_host", "rho_in_host"):
+            if hasattr(self, name):
+                setattr(self, name, None)
+        self.torch.cuda.empty_cache()
+
     # ---- small helpers -----------------------------------------------------
     def _dev(self, a):
         return self.torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.dev)
@@ -253,8 +263,20 @@ class Scf:
         rho = self.lincomb([raw], [1.0], self._zeros(), take_abs=True)
         return rho, (G, Uq, r, raw)
 
-    def run(self, callback=None, rho0=None):
+    def iterate(self, rho0=None, max_iter=None, tol=None, host_io=False):
+        """The SCF loop as a generator: yields each iteration's record and
+        stops once |E_k - E_{k-1}| / n_atoms < tol (cfg.tol_e_atom unless
+        given) or after max_iter iterations.  The current eigenvectors,
+        eigenvalues and output density are kept in self.X, self.eigenvalues
+        and self.rho after every iteration.
+
+        host_io: the densities live on the host between iterations, as in
+        the reference's driver: each iteration's rho_in goes through a pinned
+        host buffer (device -> host -> device) and rho_out is read back to
+        pinned host memory (self.rho_host)."""
         cfg, torch = self.cfg, self.torch
+        max_iter = cfg.max_iter if max_iter is None else max_iter
+        tol = cfg.tol_e_atom if tol is None else tol
         k, m = self.k, self.m
         kT = KB_HA_PER_K * cfg.temperature
         X = api.Mat(self.op, k, np.random.default_rng(cfg.seed).standard_normal((self.s.N, k)))
@@ -266,12 +288,10 @@ class Scf:
         lower_wanted = lower_unwanted = None
         occ_energy = 1e9
         e_old = None
-        history = []
         rho_in = self.initial_density() if rho0 is None else rho0
         sch = cheb_schedule(cfg, m)
-        t_start = time.perf_counter()
         w = None
-        for it in range(cfg.max_iter):
+        for it in range(max_iter):
             t_it = time.perf_counter()
             ph = {}
             mark = [t_it]
@@ -285,6 +305,12 @@ class Scf:
             if it > 0:
                 rho_in = self.anderson(hist_in, hist_out)
                 lap("mixing")
+            if host_io:
+                if getattr(self, "rho_host", None) is None:
+                    self.rho_in_host = torch.empty(self.nq, dtype=torch.float64, pin_memory=True)
+                    self.rho_host = torch.empty(self.nq, dtype=torch.float64, pin_memory=True)
+                self.rho_in_host.copy_(rho_in)
+                rho_in = self.rho_in_host.to(self.dev, non_blocking=True)
             veff = self.veff_from(rho_in)
             lap("veff")
             self.update_hamiltonian(veff)
@@ -334,6 +360,8 @@ class Scf:
             energy = e_band + e_grid + self.e_nn
             drho = self.lincomb([rho_out, rho_in], [1.0, -1.0], self._zeros())
             drho2 = self.integrate(drho, drho)
+            if host_io:
+                self.rho_host.copy_(rho_out)
             lap("energy")
             hist_in.append(rho_in)
             hist_out.append(rho_out)
@@ -344,21 +372,27 @@ class Scf:
             rec = {"iter": it, "energy": energy, "e_atom": energy / self.natoms, "de_atom": de,
                    "drho2": drho2, "fermi": mu, "eig_lowest": float(w[0]),
                    "veff_ranks": list(self.veff_ranks), "s": time.perf_counter() - t_it,
-                   "phases": ph, "passes": n_pass, "cheb_err": errs, "rho_ranks": list(r), "eig_top": float(w[-1]),
-                   "upper": upper, "n_out": self.integrate(rho_out)}
+                   "phases": ph, "passes": n_pass, "cheb_err": errs, "rho_ranks": list(r),
+                   "eig_top": float(w[-1]), "upper": upper, "n_out": self.integrate(rho_out)}
+            self.eigenvalues, self.X, self.rho = w, X, rho_out
+            self.upper_bound = upper
+            e_old = energy
+            yield rec
+            if de is not None and de < tol:
+                break
+
+    def run(self, callback=None, rho0=None):
+        """Runs the SCF loop to convergence (or cfg.max_iter)."""
+        t_start = time.perf_counter()
+        history = []
+        for rec in self.iterate(rho0):
             history.append(rec)
             if callback:
                 callback(rec)
-            e_old = energy
-            if de is not None and de < cfg.tol_e_atom:
-                break
-        torch.cuda.synchronize()
-        self.eigenvalues = w
-        self.X = X
-        self.rho = hist_out[-1]
+        self.torch.cuda.synchronize()
         return {"history": history, "energy": history[-1]["energy"],
                 "iterations": len(history), "converged": history[-1]["de_atom"] is not None
-                and history[-1]["de_atom"] < cfg.tol_e_atom,
+                and history[-1]["de_atom"] < self.cfg.tol_e_atom,
                 "wall_s": time.perf_counter() - t_start}
 
     def anderson(self, hin, hout):
