@@ -171,28 +171,17 @@ class Timer:
         self.s = self.e0.elapsed_time(self.e1) / 1e3
 
 
-def time_to_scf(s, filt, rho0=None, label=None):
+def time_to_scf(s, filt, guess="sad"):
     from ttdft_public_gb300 import scf
-    g = scf.Scf(s, scf_config(filt))
+    g = scf.Scf(s, scf_config(filt, guess=guess))
     with Timer() as t:
-        res = g.run(rho0=rho0)
+        res = g.run()
     h = res["history"]
     out = {"s": round(t.s, 3), "iterations": res["iterations"], "converged": res["converged"],
            "energy_ha": res["energy"], "s_per_iter": round(t.s / res["iterations"], 4),
-           "filter_passes": int(sum(r["passes"] for r in h))}
+           "filter_passes": int(sum(r["passes"] for r in h)), "guess": g.guess_used,
+           "start_density_error": round(g.start_error(), 5)}
     return out, g
-
-
-def learned_guess(s):
-    """rho0 from the trained initial-guess network, or None without a model."""
-    try:
-        from ttdft_public_gb300 import learned
-    except ImportError:
-        return None, None
-    model = learned.load_default()
-    if model is None:
-        return None, None
-    return model, learned.initial_density_for(s, model)
 
 
 def run_ours(args, rank, world):
@@ -270,11 +259,12 @@ def run_ours(args, rank, world):
         g64.close()
         del g64
         tts["fp64"]["de_atom_vs_mixed"] = abs(tts["fp64"]["energy_ha"] - tts["mixed"]["energy_ha"]) / s.spec.n_atoms
-    model, rho0 = learned_guess(s)
-    if rho0 is not None:
-        tts["mixed_learned"], gl = time_to_scf(s, "mixed", rho0=rho0)
+    from ttdft_public_gb300 import learned
+    if learned.load_default() is not None:
+        tts["mixed_learned"], gl = time_to_scf(s, "mixed", guess="learned")
         gl.close()
         del gl
+        log("time to SCF, mixed + learned guess:", tts["mixed_learned"])
         tts["mixed_learned"]["de_atom_vs_mixed"] = abs(
             tts["mixed_learned"]["energy_ha"] - tts["mixed"]["energy_ha"]) / s.spec.n_atoms
 

@@ -326,6 +326,39 @@ ttg_status ttg_hartree_energy(int32_t K, const double* alpha, const double* omeg
                               const double* ux, const double* uy, const double* uz,
                               double* energy);
 
+/* ---- learned initial density (no counterpart in the reference; its guess
+ * is the superposition of atomic densities, dft/InitialGuess.cc:573-681,
+ * which stays the fallback) --------------------------------------------- */
+
+/* Pairwise Gaussian radial descriptors of each atom (pos: natoms x 3, bohr):
+ *   out[a][m] = sum_{b != a} exp(-eta (r_ab - mu_m)^2) fc(r_ab),
+ *   mu_m = mu0 + m dmu, fc(r) = (cos(pi r / rc) + 1) / 2 for r < rc.
+ * out: natoms x n_features, host memory. */
+ttg_status ttg_atom_descriptors(int32_t natoms, const double* pos, int32_t n_features, double mu0,
+                                double dmu, double eta, double rc, float* out);
+
+/* Multilayer perceptron, FP32: sizes[0..n_layers], tanh hidden layers, linear
+ * output; parameters packed per layer as W (in x out, row-major) then b. */
+typedef struct ttg_mlp ttg_mlp;
+ttg_status ttg_mlp_create(int32_t n_layers, const int32_t* sizes, ttg_mlp** out);
+void ttg_mlp_destroy(ttg_mlp* m);
+int64_t ttg_mlp_num_params(const ttg_mlp* m);
+/* Host FP32 parameter vectors; set also resets the optimiser state. */
+ttg_status ttg_mlp_set_params(ttg_mlp* m, const float* p);
+ttg_status ttg_mlp_get_params(ttg_mlp* m, float* p);
+/* y (n x out) = network(x (n x in)), host arrays. */
+ttg_status ttg_mlp_forward(ttg_mlp* m, const float* x, int32_t n, float* y);
+/* Loss = mean over samples of sum_j (y_j - t_j)^2 and its gradient with
+ * respect to the parameters (host arrays). */
+ttg_status ttg_mlp_gradients(ttg_mlp* m, const float* x, const float* t, int32_t n, float* grad,
+                             float* loss);
+/* Minibatch Adam (decoupled weight decay on the weights) for `epochs` passes
+ * over (x, t); samples reshuffled every epoch from `seed`; the mean loss of
+ * each epoch into loss_per_epoch (may be NULL). */
+ttg_status ttg_mlp_train(ttg_mlp* m, const float* x, const float* t, int32_t n, int32_t epochs,
+                         int32_t batch, float lr, float weight_decay, uint64_t seed,
+                         float* loss_per_epoch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,80 @@
+"""The learned initial guess on the GPU: descriptor, forward and gradient
+kernels against the CPU oracle, training, and the gain of the packaged model
+over the superposition guess on a configuration outside its training set."""
+import numpy as np
+import pytest
+
+from oracle import mlp as omlp
+from ttdft_public_gb300 import learned
+
+pytestmark = pytest.mark.gpu
+
+
+def test_descriptors_match_oracle():
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(0, 14, (20, 3))
+    d = learned.descriptors(pos)
+    ref = omlp.descriptors(pos, learned.N_FEATURES, learned.MU0, learned.DMU, learned.ETA,
+                           learned.RCUT)
+    assert np.abs(d - ref).max() < 1e-5 * max(1.0, np.abs(ref).max())
+
+
+def test_forward_and_gradients_match_oracle():
+    rng = np.random.default_rng(4)
+    sizes = [32, 64, 64, 8]
+    p = learned.init_params(sizes, seed=1) + rng.standard_normal(learned.n_params(sizes)).astype(
+        np.float32) * 0.05
+    x = rng.standard_normal((100, 32)).astype(np.float32)
+    t = rng.standard_normal((100, 8)).astype(np.float32)
+    net = learned.Net(sizes, p)
+    try:
+        y = net.forward(x)
+        loss, g = net.gradients(x, t)
+    finally:
+        net.close()
+    yr = omlp.forward(p, sizes, x)[-1]
+    lr_, gr = omlp.loss_and_grad(p.astype(np.float64), sizes, x.astype(np.float64),
+                                 t.astype(np.float64))
+    assert np.abs(y - yr).max() < 1e-5 * max(1.0, np.abs(yr).max())
+    assert abs(loss - lr_) < 1e-5 * lr_
+    # FP32 kernels against the FP64 oracle
+    assert np.abs(g - gr).max() < 1e-4 * np.abs(gr).max()
+
+
+def test_training_fits_a_smooth_function():
+    rng = np.random.default_rng(5)
+    sizes = [4, 32, 32, 2]
+    x = rng.uniform(-1, 1, (512, 4)).astype(np.float32)
+    t = np.stack([np.sin(2 * x[:, 0]) * x[:, 1], np.cos(x[:, 2] + x[:, 3])], 1).astype(np.float32)
+    net = learned.Net(sizes, learned.init_params(sizes, seed=2))
+    try:
+        loss0, _ = net.gradients(x, t)
+        hist = net.train(x, t, epochs=300, batch=64, lr=3e-3, weight_decay=0.0, seed=1)
+        loss1, _ = net.gradients(x, t)
+    finally:
+        net.close()
+    assert hist[-1] < 0.05 * hist[0]
+    assert loss1 < 0.05 * loss0
+
+
+@pytest.mark.skipif(learned.load_default() is None, reason="no trained model packaged")
+def test_learned_guess_gains_over_superposition():
+    """A held-out 16-atom configuration, judged by the FP64 SCF: the learned
+    start is closer to the converged density, needs no more SCF iterations,
+    and both starts reach the same energy (both converged to 1e-7 Ha/atom
+    between iterations, so that the slow Anderson tail leaves them well inside
+    the 1e-5 Ha/atom comparison)."""
+    from ttdft_public_gb300 import scf, system
+    s = system.build_system(learned.training_spec(16, 987654))
+    res, err = {}, {}
+    for guess in ("sad", "learned"):
+        g = scf.Scf(s, scf.ScfConfig(filter="fp64", mix_alpha=0.1, history=10, max_iter=120,
+                                     tol_e_atom=1e-7, guess=guess))
+        res[guess] = g.run()
+        assert g.guess_used == guess
+        err[guess] = g.start_error()
+        g.close()
+    assert res["sad"]["converged"] and res["learned"]["converged"]
+    assert err["learned"] < 0.7 * err["sad"], err
+    assert res["learned"]["iterations"] <= res["sad"]["iterations"]
+    assert abs(res["learned"]["energy"] - res["sad"]["energy"]) / 16 < 1e-5

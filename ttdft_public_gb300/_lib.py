@@ -96,6 +96,14 @@ _SIGS = {
     "ttg_hartree": [c_i32, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_i32, c_i32, c_i32,
                     c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32,
                     c_vp, c_vp, c_vp, c_vp, c_vp],
+    "ttg_atom_descriptors": [c_i32, c_vp, c_i32, c_dbl, c_dbl, c_dbl, c_dbl, c_vp],
+    "ttg_mlp_create": [c_i32, c_vp, c_vp],
+    "ttg_mlp_set_params": [c_vp, c_vp],
+    "ttg_mlp_get_params": [c_vp, c_vp],
+    "ttg_mlp_forward": [c_vp, c_vp, c_i32, c_vp],
+    "ttg_mlp_gradients": [c_vp, c_vp, c_vp, c_i32, c_vp, c_vp],
+    "ttg_mlp_train": [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, ctypes.c_float, ctypes.c_float,
+                      ctypes.c_uint64, c_vp],
     "ttg_hartree_energy": [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                            c_vp, c_vp, c_vp, c_vp, c_vp],
 }
@@ -105,6 +113,8 @@ _OTHER = {
     "ttg_op_stream": ([c_vp], c_vp),
     "ttg_block_cols": ([c_vp], c_i32),
     "ttg_kernel_launches": ([], c_i64),
+    "ttg_mlp_destroy": ([c_vp], None),
+    "ttg_mlp_num_params": ([c_vp], c_i64),
 }
 
 EXPORTED = sorted(list(_SIGS) + list(_OTHER))

@@ -62,6 +62,8 @@ class ScfConfig:
     ion_width: float = 1.0            # Gaussian ionic charges (bohr)
     sad_width: float = 1.0            # width of the atomic densities (bohr)
     filter: str = "fp64"              # fp64 | fp32 | mixed (BF16 first quarter)
+    guess: str = "sad"                # sad | learned (falls back to sad without a model)
+    model_path: str = ""              # learned-guess model ("" = the packaged one)
     seed: int = 0
 
 
@@ -136,12 +138,18 @@ class Scf:
         self.e_nn = repulsive_energy(sysm.atoms, spec.z_val)
         self.timings = {}
 
+    def start_error(self):
+        """|| rho_0 - rho || / || rho || (quadrature norm) of the initial guess
+        against the current output density."""
+        d = self.lincomb([self.rho_start, self.rho], [1.0, -1.0], self._zeros())
+        return math.sqrt(self.integrate(d, d) / self.integrate(self.rho, self.rho))
+
     def close(self):
         """Releases the operator and the device fields of this run."""
         if getattr(self, "op", None) is not None:
             self.op.close()
             self.op = None
-        for name in ("X", "rho", "vloc", "wq", "rho_host", "rho_in_host"):
+        for name in ("X", "rho", "rho_start", "vloc", "wq", "rho_host", "rho_in_host"):
             if hasattr(self, name):
                 setattr(self, name, None)
         self.torch.cuda.empty_cache()
@@ -230,6 +238,16 @@ class Scf:
              for d in range(3)]
         rho = self._zeros()
         self._cp_sum(norm * np.ones(self.natoms), f, rho, self.qdims, accumulate=False)
+        self.guess_used = "sad"
+        if cfg.guess == "learned":
+            from . import learned
+            model = learned.Model.load(cfg.model_path) if cfg.model_path else learned.load_default()
+            if model is not None:
+                c = model.predict(self.s.atoms)
+                fc = learned.correction_factors(self.s.atoms, self.xq)
+                self._cp_sum(c.reshape(-1), fc, rho, self.qdims, accumulate=True)
+                self.lincomb([rho], [1.0], rho, take_abs=True)
+                self.guess_used = "learned"
         rho *= self.ne / self.integrate(rho)                       # main.cc:674-680
         return rho
 
@@ -289,6 +307,7 @@ class Scf:
         occ_energy = 1e9
         e_old = None
         rho_in = self.initial_density() if rho0 is None else rho0
+        self.rho_start = rho_in
         sch = cheb_schedule(cfg, m)
         w = None
         for it in range(max_iter):
