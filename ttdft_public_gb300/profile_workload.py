@@ -1,7 +1,7 @@
 """Run a few hot-path launches of one workload, for profilers.
 
     python -m ttdft_public_gb300.profile_workload --workload atoms64 \
-        --prec fp32,bf16 --degrees 1 [--rr]
+        --prec fp32,bf16 --degrees 1 [--rr] [--states K]
     python -m ttdft_public_gb300.profile_workload --workload atoms64 --scf 1 \
         [--filter mixed]
 
@@ -31,6 +31,7 @@ def main():
     ap.add_argument("--rr", action="store_true")
     ap.add_argument("--scf", type=int, default=0)
     ap.add_argument("--filter", default="mixed", choices=("fp64", "fp32", "mixed"))
+    ap.add_argument("--states", type=int, default=0, help="block width (default: the workload's)")
     args = ap.parse_args()
     s = system.build_system(system.CONFIGS[args.workload],
                             cache_dir=os.environ.get("TTG_CACHE"))
@@ -41,7 +42,7 @@ def main():
             print("iter", h["iter"], "energy", h["energy"], "s", round(h["s"], 3),
                   {k: round(v, 3) for k, v in h["phases"].items()})
         return
-    k = s.spec.n_states
+    k = args.states or s.spec.n_states
     op = api.Operator(api.ProjectHamiltonianSparse.from_system(s), k)
     X = api.Mat(op, k, np.random.default_rng(0).standard_normal((s.N, k)))
     ax = api.AX(1, k)
