@@ -6,7 +6,9 @@
  * ttg_status; nothing terminates the process.  One CUDA stream per ttg_op;
  * calls on one handle are not thread-safe, calls on different handles are.
  * Entry points that return data in host memory synchronise the op's stream;
- * the others only enqueue work.
+ * the others only enqueue work.  The library's streams are blocking streams:
+ * work the caller enqueued on the legacy default stream before a call (for
+ * example filling an input buffer) completes before the call's kernels run.
  *
  * Layout conventions (those of the reference's PETSc dense Mats):
  *   - a vector block X is N x k, column-major (one column per state), ld >= N;

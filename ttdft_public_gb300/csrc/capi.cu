@@ -122,7 +122,7 @@ ttg_status ttg_op_create_tucker(int64_t n, const int64_t* h_row_ptr, const int32
     ttg_op_destroy(op);
     return s;
   };
-  if (cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&op->stream, cudaStreamDefault) != cudaSuccess)
     return fail(TTG_CUDA_ERR);
   for (int i = 0; i < kMaxSlots; ++i)
     if (cudaEventCreate(&op->ev[i]) != cudaSuccess) return fail(TTG_CUDA_ERR);

@@ -251,7 +251,7 @@ ttg_status ttg_mlp_create(int32_t n_layers, const int32_t* sizes, ttg_mlp** out)
     delete m;
     return s;
   }
-  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamDefault) != cudaSuccess) {
     delete m;
     return TTG_CUDA_ERR;
   }
@@ -383,7 +383,7 @@ ttg_status ttg_atom_descriptors(int32_t natoms, const double* pos, int32_t n_fea
                                 double dmu, double eta, double rc, float* out) {
   if (natoms <= 0 || !pos || n_features <= 0 || !out || rc <= 0.0) return TTG_BAD_ARG;
   cudaStream_t st;
-  TTG_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  TTG_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamDefault));
   ttg_status s = TTG_OK;
   {
     ttg::DevBuf dp, dout;

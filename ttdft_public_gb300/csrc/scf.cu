@@ -462,7 +462,7 @@ struct Stream {
     if (st) {
       s = static_cast<cudaStream_t>(st);
     } else {
-      cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+      cudaStreamCreateWithFlags(&s, cudaStreamDefault);
       own = true;
     }
   }

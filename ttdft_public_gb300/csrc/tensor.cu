@@ -365,7 +365,7 @@ ttg_status ttg_hartree(int32_t K, const double* alpha, const double* omega, int3
   int32_t smc, ma, mi;
   TTG_TRY(ttg_device_query(&smc, &ma, &mi));
   cudaStream_t st;
-  TTG_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  TTG_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamDefault));
   struct StreamGuard {
     cudaStream_t s;
     ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); }

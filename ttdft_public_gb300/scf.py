@@ -329,7 +329,7 @@ class Scf:
                     self.rho_in_host = torch.empty(self.nq, dtype=torch.float64, pin_memory=True)
                     self.rho_host = torch.empty(self.nq, dtype=torch.float64, pin_memory=True)
                 self.rho_in_host.copy_(rho_in)
-                rho_in = self.rho_in_host.to(self.dev, non_blocking=True)
+                rho_in = self.rho_in_host.to(self.dev)
             veff = self.veff_from(rho_in)
             lap("veff")
             self.update_hamiltonian(veff)
