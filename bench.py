@@ -45,6 +45,11 @@ METRIC = "s/SCF-iter & time-to-SCF @\u0394E<1e-5 Ha/atom: mixed+learned vs FP64,
 WORKLOAD = "atoms64"
 MIX_ALPHA = 0.1          # Anderson mixing parameter of this workload (input parameter)
 MIX_DEPTH = 10           # Anderson history (the reference example's history=10)
+# DRAM bytes per 64-row column slot of one FP32 filter degree, measured by
+# ncu on the 8-atom operator with a 160-column block (profile_workload
+# --workload atoms8 --states 160: 112.3 MB read + 3.7 MB written over 410,304
+# slots); scaled to the timed operator's slots
+TRAFFIC_PER_SLOT_FP32 = (112.280576e6 + 3.688448e6) / 410304
 MAX_ITER = 60
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
@@ -304,7 +309,10 @@ def run_ours(args, rank, world):
                          "degree: 3xTF32 tensor-core SpMM fused with the recurrence)",
                          "achieved": r32["achieved"], "peak": peak,
                          "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s",
-                         "frac": r32["achieved"] / peak, "traffic": None,
+                         "frac": r32["achieved"] / peak,
+                         "traffic": TRAFFIC_PER_SLOT_FP32 * info["tile_slots"],
+                         "traffic_note": "ncu DRAM bytes per slot of the 8-atom capture x this "
+                                         "operator's tile slots",
                          "bytes_per_launch": r32["bytes_per_launch"],
                          "flops_per_launch": r32["flops_per_launch"],
                          "launch_ms": r32["launch_ms"]},
