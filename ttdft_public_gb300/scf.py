@@ -89,7 +89,10 @@ def potential_matrices(basis, U):
     points (ProjectHamiltonianSparse::computeOverlapPotentialTuckerBasis,
     dft/ProjectHamiltonianSparse.cc:678-775); (r_a, r, r)."""
     B = basis.quad * basis.fem.wJ[:, None]
-    return np.ascontiguousarray(np.einsum("qi,qa,qj->aij", B, U, basis.quad, optimize=True))
+    q, r = basis.quad.shape
+    # one GEMM over the quadrature points: (r_a x q) (q x r*r)
+    M = (B[:, :, None] * basis.quad[:, None, :]).reshape(q, r * r)
+    return np.ascontiguousarray((U.T @ M).reshape(U.shape[1], r, r))
 
 
 class Scf:
