@@ -75,6 +75,8 @@ typedef struct {
   int64_t n_tiles;        /* 64-row tiles of the tensor-core format (0: none) */
   int64_t tile_slots;     /* merged column slots over all tiles */
   double tile_fill;       /* (nnz_h + nnz_c^T) / (64 * tile_slots) */
+  int64_t umma_tiles;     /* 128-row tiles of the tcgen05 format (0: none) */
+  int64_t umma_slots;     /* merged column slots over those tiles */
 } ttg_op_info_t;
 
 /* ---- device and operator ------------------------------------------------ */
@@ -118,6 +120,8 @@ ttg_status ttg_op_destroy(ttg_op* op);
 ttg_status ttg_op_info(const ttg_op* op, ttg_op_info_t* info);
 /* The op's cudaStream_t, as an opaque pointer, for callers that overlap work. */
 void* ttg_op_stream(ttg_op* op);
+/* Waits for the op's stream; TTG_TIMEOUT if a bounded wait inside a
+ * tensor-memory filter kernel ran out since the last check. */
 ttg_status ttg_op_sync(ttg_op* op);
 /* Device-side timing on the op's stream (slot 0..15). */
 ttg_status ttg_op_record(ttg_op* op, int32_t slot);

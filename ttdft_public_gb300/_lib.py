@@ -45,7 +45,8 @@ class TtgOpInfo(ctypes.Structure):
     _fields_ = [("n", c_i64), ("nnz_h", c_i64), ("nnz_c", c_i64), ("nproj", c_i32),
                 ("group_rows", c_i32), ("n_groups", c_i64), ("stored_cols", c_i64),
                 ("fill", c_dbl), ("device_bytes", c_i64), ("launches", c_i64),
-                ("n_tiles", c_i64), ("tile_slots", c_i64), ("tile_fill", c_dbl)]
+                ("n_tiles", c_i64), ("tile_slots", c_i64), ("tile_fill", c_dbl),
+                ("umma_tiles", c_i64), ("umma_slots", c_i64)]
 
 
 class TtgSched(ctypes.Structure):

@@ -134,6 +134,9 @@ ttg_status ttg_op_create_tucker(int64_t n, const int64_t* h_row_ptr, const int32
   if (!op->tc_disabled) {
     s = build_tiles(op, n, h_row_ptr, h_col, h_val, nproj, c_row_ptr, c_col, c_val, tucker_ranks);
     if (s != TTG_OK) return fail(s);
+    s = build_umma_tiles(op, n, h_row_ptr, h_col, h_val, nproj, c_row_ptr, c_col, c_val,
+                         tucker_ranks);
+    if (s != TTG_OK) return fail(s);
   }
   const int64_t kmax = std::max<int64_t>(max_k, kMaxLanczos);
   if ((s = ensure(op->kk0, kmax * kmax * 8, op)) != TTG_OK) return fail(s);
@@ -189,6 +192,8 @@ ttg_status ttg_op_info(const ttg_op* op, ttg_op_info_t* info) {
   info->tile_fill = op->tiles.slots > 0
                         ? (double)(op->nnz_h + op->nnz_c) / (64.0 * op->tiles.slots)
                         : 0.0;
+  info->umma_tiles = op->umma.n_tiles;
+  info->umma_slots = op->umma.slots;
   return TTG_OK;
 }
 
@@ -203,7 +208,7 @@ ttg_status ttg_op_set_rr_precision(ttg_op* op, int32_t prec) {
 ttg_status ttg_op_sync(ttg_op* op) {
   if (!op) return TTG_BAD_ARG;
   TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
-  return TTG_OK;
+  return umma_check_error(op);
 }
 
 ttg_status ttg_op_record(ttg_op* op, int32_t slot) {
@@ -527,6 +532,7 @@ ttg_status ttg_lanczos_bounds(ttg_op* op, const double* v0_host, int32_t max_ite
 ttg_status ttg_chfsi_pass(ttg_op* op, ttg_block* X, int32_t m, double a, double b, double a0,
                           ttg_sched sched, int32_t rotate, double* w_host) {
   TTG_TRY(ttg_cheb_filter(op, X, m, a, b, a0, sched));
+  TTG_TRY(umma_check_error(op));
   TTG_TRY(ttg_chol_qr(op, X));
   return ttg_rayleigh_ritz(op, X, rotate, w_host, nullptr);
 }

@@ -46,6 +46,8 @@ struct UpdateArgs {
   __nv_bfloat16* v16;
   float* t32;
   __nv_bfloat16* t16;
+  const int* umma_pos;        // element of the entry in plane 0 of the 128-row tiles
+  __nv_bfloat16* u16;         // their three BF16 planes (2048 elements apart)
   int64_t n;
 };
 
@@ -100,6 +102,16 @@ __global__ void k_update_values(UpdateArgs a) {
       const int j = a.tile_slot[e];
       a.t32[(int64_t)(base + (j & 3)) * 4 + (j >> 2)] = (float)val;
       a.t16[(int64_t)(base + ((j & 7) >> 1)) * 4 + (j & 1) + 2 * (j >> 3)] = __double2bfloat16(val);
+    }
+    if (a.u16) {
+      // three BF16 terms, as the tile builder splits them
+      __nv_bfloat16* u = a.u16 + a.umma_pos[e];
+      const __nv_bfloat16 h0 = __float2bfloat16_rn((float)val);
+      const double r1 = val - (double)__bfloat162float(h0);
+      const __nv_bfloat16 h1 = __float2bfloat16_rn((float)r1);
+      u[0] = h0;
+      u[2048] = h1;
+      u[4096] = __float2bfloat16_rn((float)(r1 - (double)__bfloat162float(h1)));
     }
   }
 }
@@ -199,6 +211,8 @@ ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const d
   a.v16 = op->rg.v16.as<__nv_bfloat16>();
   a.t32 = op->tiles.n_tiles > 0 && P.tile_base.p ? op->tiles.v32.as<float>() : nullptr;
   a.t16 = op->tiles.v16.as<__nv_bfloat16>();
+  a.umma_pos = P.umma_pos.as<int>();
+  a.u16 = op->umma.n_tiles > 0 && P.umma_pos.p ? op->umma.hpl.as<__nv_bfloat16>() : nullptr;
   a.n = op->n;
   const int wpb = 8;
   k_update_values<<<(unsigned)((op->n + wpb - 1) / wpb), 32 * wpb, 0, st>>>(a); TTG_COUNT();

@@ -692,6 +692,8 @@ static ttg_status launch_step_t(ttg_op* op, const TV* vals, const void* src, con
 ttg_status launch_cheb_step(ttg_op* op, int prec, const void* src, const void* xold, void* dst,
                             int k, double alpha, double beta, double delta) {
   if (k <= 0 || k > op->max_k) return TTG_BAD_ARG;
+  if (umma_supported(op, prec, k))
+    return launch_cheb_umma(op, src, xold, dst, k, alpha, beta, delta);
   if (tc_supported(op, prec, k))
     return launch_cheb_tc(op, prec, src, xold, dst, k, alpha, beta, delta);
   if (prec == TTG_PREC_FP64) {

@@ -110,6 +110,20 @@ struct TileOp {
   DevBuf v16;      // bf16,  [chunk][8 n-tiles][32 lanes][4]
 };
 
+// 128-row tiles for the tcgen05 FP32 filter degree (spmm_umma.cu): H as three
+// BF16 planes per 16-slot chunk in the MMA operand layout, and the block's
+// three BF16 planes that the kernel gathers.
+struct UmmaOp {
+  int64_t n_tiles = 0;
+  int64_t slots = 0;
+  DevBuf tptr;     // int64 [n_tiles+1], slot offsets (multiples of 16)
+  DevBuf tcol;     // int32 [slots]
+  DevBuf rowmap;   // int32 [n_tiles*128], -1 = padding
+  DevBuf hpl;      // bf16 [chunk][3][128 x 16]
+  DevBuf xpl;      // bf16 [3][n + nproj][k]
+  DevBuf err;      // int: a bounded wait of the kernel ran out
+};
+
 // The fixed sparsity pattern of H_loc and where each entry lives in the device
 // formats, kept when the operator is created with Tucker ranks so that its
 // values can be recomputed on the device for a new potential (hupdate.cu).
@@ -119,6 +133,7 @@ struct Pattern {
   DevBuf rg_pos;     // int32 [nnz]: index into the row-group value arrays
   DevBuf tile_base;  // int32 [nnz]: lane base of the entry's tile fragment
   DevBuf tile_slot;  // uint8 [nnz]: slot of the entry within its 16-slot chunk
+  DevBuf umma_pos;   // int32 [nnz]: element of the entry in plane 0 of the 128-row tiles
   int32_t r[3] = {0, 0, 0};   // Tucker ranks of the basis
   int32_t bw[3] = {0, 0, 0};  // max |coordinate difference| per direction over the entries
   DevBuf kin;        // 6 r x r 1-D matrices: DX DY DZ MX MY MZ (row-major)
@@ -146,6 +161,7 @@ struct ttg_op {
   int64_t nnz_h = 0, nnz_c = 0;
   ttg::RowGroups rg;
   ttg::TileOp tiles;          // tensor-core format (FP32/BF16 degrees)
+  ttg::UmmaOp umma;           // tcgen05 format (FP32 degrees)
   bool tc_disabled = false;   // TTG_DISABLE_TC=1: CUDA-core kernels only
   bool keep_pattern = false;  // Tucker ranks given: keep the pattern for value updates
   ttg::Pattern pattern;
@@ -193,6 +209,14 @@ ttg_status build_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int32_t* 
                        const double* hv, int32_t nproj, const int64_t* cp, const int32_t* cc,
                        const double* cv, const int32_t* dims);
 bool tc_supported(const ttg_op* op, int prec, int k);
+// spmm_umma.cu
+ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int32_t* hc,
+                            const double* hv, int32_t nproj, const int64_t* cp, const int32_t* cc,
+                            const double* cv, const int32_t* dims);
+bool umma_supported(const ttg_op* op, int prec, int k);
+ttg_status launch_cheb_umma(ttg_op* op, const void* src, const void* xold, void* dst, int k,
+                            double alpha, double beta, double delta);
+ttg_status umma_check_error(ttg_op* op);
 ttg_status launch_cheb_tc(ttg_op* op, int prec, const void* src, const void* xold, void* dst,
                           int k, double alpha, double beta, double delta);
 ttg_status launch_convert(ttg_op* op, int from, int to, const void* src, void* dst,
