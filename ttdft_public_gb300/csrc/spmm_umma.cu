@@ -22,13 +22,15 @@
 //  - Y: the 16 source rows are gathered from three BF16 planes of the block
 //    (written by k_split3 before the launch) into the canonical MN-major
 //    layout with 16-byte cp.async copies.
-// Warp-specialised pipeline: eleven producer warps fill the stages (the H
-// block by TMA, the gathered rows by cp.async whose completion arrives on the
-// stage's mbarrier); one thread of warp 1 issues the six MMAs of a
-// chunk as soon as the stage is full and commits them to the stage's "done"
-// mbarrier, after which the producers refill it.  As many stages as fit in
-// shared memory (8 for 160 states, one CTA per SM).  The epilogue reads the accumulator from
-// tensor memory (one warp per 32 rows) and applies the recurrence in FP32.
+// Warp-specialised pipeline: up to nine producer warps take whole chunks in
+// turn and fill their stage (the H block by TMA; the gathered rows by cp.async,
+// which the warp waits for and fences for the async proxy before it signals
+// the stage's mbarrier); one thread of warp 1 issues the six MMAs of a chunk
+// as soon as the stage is full and commits them to the stage's "done"
+// mbarrier, after which the stage is refilled.  As many stages as fit in
+// shared memory (8 for 160 states, one CTA per SM).  The epilogue reads the
+// accumulator from tensor memory (one warp per 32 rows) and applies the
+// recurrence in FP32.
 // Every mbarrier wait is bounded; a wait that runs out sets an error word.
 
 #include <cuda_bf16.h>
@@ -53,10 +55,11 @@ constexpr int CHUNK_ELEMS = 3 * PLANE_ELEMS;  // three planes
 constexpr int CHUNK_BYTES = 2 * CHUNK_ELEMS;  // 12288
 constexpr int kMaxStages = 8;                // pipeline depth: as many as fit in shared memory
 constexpr int kSmemBudget = 227 * 1024 - 1024;
-constexpr int kThreads = 384;                // 12 warps
-constexpr int kProducerWarps = 11;            // every warp but warp 1 loads
+constexpr int kThreads = 320;                // 10 warps
+constexpr int kProducerWarps = 9;             // every warp but warp 1 loads (at most nst of them)
 constexpr int kMmaWarp = 1;                   // warp 1 issues the MMAs
 constexpr int kMaxWait = 1 << 20;
+constexpr int kColAhead = 4;                  // chunks per warp whose column indices are loaded ahead
 
 // Canonical no-swizzle layouts (8 x 16-byte core matrices, 128 bytes each):
 // core matrices 128 bytes apart along K and 256 bytes apart along M / N.
@@ -112,15 +115,18 @@ __device__ __forceinline__ void cp_async_wait() {
 
 __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     const int64_t* __restrict__ tptr, const int* __restrict__ tcol, const int* __restrict__ rowmap,
-    const __nv_bfloat16* __restrict__ hpl, const __nv_bfloat16* __restrict__ xpl,
+    const int* __restrict__ order, const __nv_bfloat16* __restrict__ hpl, const __nv_bfloat16* __restrict__ xpl,
     int64_t pstride, int ps, const float* __restrict__ src, const float* xold, float* dst,
     int k, int64_t ld, float alpha, float beta, float delta,
     uint32_t tmem_cols, int nst, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[kMaxStages];
   __shared__ __align__(8) uint64_t mdone[kMaxStages];
+  __shared__ __align__(8) uint64_t accf;     // all MMAs of the tile done (one phase)
   __shared__ uint32_t tmem_slot;
-  const int tile = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // tiles in decreasing chunk count, so the longest start first and the short
+  // ones fill the tail of the launch
+  const int tile = __ldg(order + blockIdx.x), tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int stage_bytes = CHUNK_BYTES + 96 * k;          // H planes + 3 block planes
   const int64_t c_first = tptr[tile] / UK;
   const int nch = (int)((tptr[tile + 1] - tptr[tile]) / UK);
@@ -133,9 +139,10 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
   }
   if (tid == 0) {
     for (int s = 0; s < nst; ++s) {
-      mbar_init(&full[s], kProducerWarps * 32 + 1);   // producer threads + the H copy's expect_tx
+      mbar_init(&full[s], 2);                    // the owning warp: H copy's expect_tx + rows fenced
       mbar_init(&mdone[s], 1);                   // one tcgen05.commit
     }
+    mbar_init(&accf, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -145,40 +152,76 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
   bool ok = true;
 
   if (warp != kMmaWarp) {
-    // producers: every warp but warp 1.  Chunk c goes into stage c % nst once the
-    // MMAs of chunk c - nst have read it.  Every producer thread's copies
-    // arrive on the stage's mbarrier when they complete
-    // (cp.async.mbarrier.arrive.noinc), the H block by its byte count.
+    // producers: warps 0, 2, 3, ... (pw = 0 .. np-1) take whole chunks in turn,
+    // chunk c to warp c % np.  Chunk c goes into stage c % nst once the MMAs of
+    // chunk c - nst have read it; np <= nst keeps every waiter within one phase
+    // of the stage's "done" barrier (a warp's previous chunk c - np waited for
+    // chunk c - np - nst >= c - 2 nst).  The owning warp arrives on the stage's
+    // "full" barrier once its row copies have landed and are fenced; the H
+    // block completes by byte count.  A warp waits for its own copies only:
+    // the np warps fill np stages at once.
+    const int np = min(kProducerWarps, nst);
     const int pw = warp == 0 ? 0 : warp - 1;
-    const int lsl = lane & 15, lhalf = lane >> 4;
-    const int gp = (ngrp + 1) >> 1;
-    for (int c = 0; c < nch; ++c) {
-      const int s = c % nst;
-      if (c >= nst) ok &= mbar_wait(&mdone[s], ((c / nst) - 1) & 1);
-      unsigned char* st = smem + s * stage_bytes;
-      if (pw == 0 && lane == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                     ::"r"(smem_u32(&full[s])), "r"(CHUNK_BYTES) : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-            ::"r"(smem_u32(st)), "l"(hpl + (c_first + c) * CHUNK_ELEMS), "r"(CHUNK_BYTES),
-            "r"(smem_u32(&full[s]))
-            : "memory");
+    if (pw < np) {
+      const int lsl = lane & 15, lhalf = lane >> 4;
+      // lane = slot (16) x half (2) of a 32-byte sector: one instruction writes
+      // 512 contiguous bytes of shared memory
+      const __nv_bfloat16* xl = xpl + 8 * lhalf;
+      const uint32_t dl = (uint32_t)(lhalf * 256 + lsl * 16);
+      const int* colp = tcol + c_first * UK + lsl;
+      // column indices of this warp's next kColAhead chunks live in registers
+      int cur[kColAhead], nxt[kColAhead];
+#pragma unroll
+      for (int j = 0; j < kColAhead; ++j) {
+        const int c = pw + j * np;
+        cur[j] = c < nch ? __ldg(colp + (int64_t)c * UK) : 0;
       }
-      // B pieces: lane = slot x half of a 32-byte sector; a warp writes 512
-      // contiguous bytes of shared memory per instruction
-      unsigned char* sb = st + CHUNK_BYTES;
-      const int64_t col = __ldg(tcol + (c_first + c) * UK + lsl);
-      for (int it = pw; it < 3 * gp; it += kProducerWarps) {
-        const int pl = it / gp;
-        const int g = 2 * (it - pl * gp) + lhalf;
-        if (g < ngrp)
-          cp_async16(sb + pl * (32 * k) + g * 256 + lsl * 16, xpl + pl * pstride + col * ps + 8 * g);
+      for (int c0 = pw; c0 < nch; c0 += kColAhead * np) {
+#pragma unroll
+        for (int j = 0; j < kColAhead; ++j) {
+          const int c = c0 + (kColAhead + j) * np;
+          nxt[j] = c < nch ? __ldg(colp + (int64_t)c * UK) : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < kColAhead; ++j) {
+          const int c = c0 + j * np;
+          if (c >= nch) break;
+          const int s = c % nst;
+          if (c >= nst) ok &= mbar_wait(&mdone[s], ((c / nst) - 1) & 1);
+          unsigned char* st = smem + s * stage_bytes;
+          if (lane == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         ::"r"(smem_u32(&full[s])), "r"(CHUNK_BYTES) : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                ::"r"(smem_u32(st)), "l"(hpl + (c_first + c) * CHUNK_ELEMS), "r"(CHUNK_BYTES),
+                "r"(smem_u32(&full[s]))
+                : "memory");
+          }
+          const __nv_bfloat16* xs = xl + (int64_t)cur[j] * ps;
+          const uint32_t d0 = smem_u32(st + CHUNK_BYTES) + dl;
+#pragma unroll
+          for (int pl = 0; pl < 3; ++pl)
+            for (int g = 0; g < ngrp; g += 2)   // ngrp = k / 8 is even
+              asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+                           ::"r"(d0 + (uint32_t)(pl * 32 * k + g * 256)), "l"(xs + pl * pstride + 8 * g)
+                           : "memory");
+          // the rows were written through the generic proxy: each thread waits
+          // for its own copies and fences them for the tensor core's
+          // (async-proxy) reads before the warp signals the stage
+          cp_async_commit();
+          cp_async_wait<0>();
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncwarp();
+          if (lane == 0)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full[s]))
+                         : "memory");
+        }
+#pragma unroll
+        for (int j = 0; j < kColAhead; ++j) cur[j] = nxt[j];
       }
-      asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(&full[s]))
-                   : "memory");
+      cp_async_wait<0>();
     }
-    cp_async_wait<0>();
   } else if (lane == 0) {
     // MMA issuer: six MMAs per chunk (term pairs, smallest products first)
     const uint32_t idesc = instr_desc(UR, k);
@@ -187,9 +230,6 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     for (int c = 0; c < nch; ++c) {
       const int s = c % nst;
       ok &= mbar_wait(&full[s], (c / nst) & 1);
-      // the gathered rows were written through the generic proxy: order them
-      // before the tensor core's (async-proxy) reads
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t a0 = smem_u32(smem + s * stage_bytes);
       const uint32_t b0 = a0 + CHUNK_BYTES;
@@ -208,10 +248,17 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
           ::"r"(smem_u32(&mdone[s]))
           : "memory");
     }
+    if (nch > 0)
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+          ::"r"(smem_u32(&accf))
+          : "memory");
   }
   __syncwarp();
-  // all MMAs done: the last commit tracks every earlier MMA of the issuer
-  if (nch > 0) ok &= mbar_wait(&mdone[(nch - 1) % nst], ((nch - 1) / nst) & 1);
+  // all MMAs done.  A barrier of its own, used for one phase: a thread may
+  // get here long before the last chunk's stage barrier has passed the phase
+  // before its last one, where a parity wait on it would pass early.
+  if (nch > 0) ok &= mbar_wait(&accf, 0);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   // epilogue (warps 0-3, one per 32 TMEM lanes): row = warp*32 + lane of the
@@ -381,6 +428,10 @@ ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int3
       tptr[t + 1] = ((int64_t)cols.size() + UK - 1) / UK * UK;
     }
   }
+  std::vector<int32_t> order(ntiles);
+  for (int64_t t = 0; t < ntiles; ++t) order[t] = (int32_t)t;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t a, int32_t b) { return tptr[a + 1] > tptr[b + 1]; });
   for (int64_t t = 0; t < ntiles; ++t) tptr[t + 1] += tptr[t];
   const int64_t slots = tptr[ntiles];
   const int64_t nchunk = slots / UK;
@@ -424,11 +475,14 @@ ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int3
   TTG_TRY(U.tptr.alloc((ntiles + 1) * sizeof(int64_t)));
   TTG_TRY(U.tcol.alloc(tcol.size() * sizeof(int32_t)));
   TTG_TRY(U.rowmap.alloc(rowmap.size() * sizeof(int32_t)));
+  TTG_TRY(U.order.alloc(order.size() * sizeof(int32_t)));
   TTG_TRY(U.hpl.alloc(hpl.size() * sizeof(uint16_t)));
   TTG_TRY(U.err.alloc(sizeof(int)));
   TTG_CUDA_TRY(cudaMemcpyAsync(U.tptr.p, tptr.data(), U.tptr.bytes, cudaMemcpyHostToDevice, op->stream));
   TTG_CUDA_TRY(cudaMemcpyAsync(U.tcol.p, tcol.data(), U.tcol.bytes, cudaMemcpyHostToDevice, op->stream));
   TTG_CUDA_TRY(cudaMemcpyAsync(U.rowmap.p, rowmap.data(), U.rowmap.bytes, cudaMemcpyHostToDevice,
+                               op->stream));
+  TTG_CUDA_TRY(cudaMemcpyAsync(U.order.p, order.data(), U.order.bytes, cudaMemcpyHostToDevice,
                                op->stream));
   TTG_CUDA_TRY(cudaMemcpyAsync(U.hpl.p, hpl.data(), U.hpl.bytes, cudaMemcpyHostToDevice, op->stream));
   TTG_CUDA_TRY(cudaMemsetAsync(U.err.p, 0, sizeof(int), op->stream));
@@ -439,7 +493,7 @@ ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int3
     op->device_bytes += op->pattern.umma_pos.bytes;
   }
   TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
-  op->device_bytes += U.tptr.bytes + U.tcol.bytes + U.rowmap.bytes + U.hpl.bytes;
+  op->device_bytes += U.tptr.bytes + U.tcol.bytes + U.rowmap.bytes + U.order.bytes + U.hpl.bytes;
   return TTG_OK;
 }
 
@@ -477,7 +531,8 @@ ttg_status launch_cheb_umma(ttg_op* op, const void* src, const void* xold, void*
   if (nst < 3) return TTG_BAD_ARG;
   const size_t smem = (size_t)nst * stage_bytes;
   k_cheb_umma<<<(unsigned)U.n_tiles, kThreads, smem, op->stream>>>(
-      U.tptr.as<int64_t>(), U.tcol.as<int>(), U.rowmap.as<int>(), U.hpl.as<__nv_bfloat16>(),
+      U.tptr.as<int64_t>(), U.tcol.as<int>(), U.rowmap.as<int>(), U.order.as<int>(),
+      U.hpl.as<__nv_bfloat16>(),
       U.xpl.as<__nv_bfloat16>(), pstride, ps, reinterpret_cast<const float*>(src),
       reinterpret_cast<const float*>(xold), reinterpret_cast<float*>(dst), k, op->ld,
       (float)alpha, (float)beta, (float)delta, cols, nst, U.err.as<int>()); TTG_COUNT();

@@ -119,6 +119,7 @@ struct UmmaOp {
   DevBuf tptr;     // int64 [n_tiles+1], slot offsets (multiples of 16)
   DevBuf tcol;     // int32 [slots]
   DevBuf rowmap;   // int32 [n_tiles*128], -1 = padding
+  DevBuf order;    // int32 [n_tiles], launch order: most chunks first
   DevBuf hpl;      // bf16 [chunk][3][128 x 16]
   DevBuf xpl;      // bf16 [3][n + nproj][k]
   DevBuf err;      // int: a bounded wait of the kernel ran out
