@@ -17,20 +17,26 @@
 // Data movement per chunk.
 //  - H: the three BF16 planes of the chunk (128 x 16 values each, already in
 //    the canonical K-major no-swizzle layout of the MMA operand) are one
-//    contiguous 12 KB block, copied by one bulk asynchronous copy (TMA)
-//    that completes on an mbarrier.
+//    contiguous 12 KB block, copied by one bulk asynchronous copy (TMA,
+//    L2 evict-first) into the H ring.
 //  - Y: the 16 source rows are gathered from three BF16 planes of the block
-//    (written by k_split3 before the launch) into the canonical MN-major
-//    layout with 16-byte cp.async copies.
-// Warp-specialised pipeline: up to nine producer warps take whole chunks in
-// turn and fill their stage (the H block by TMA; the gathered rows by cp.async,
-// which the warp waits for and fences for the async proxy before it signals
-// the stage's mbarrier); one thread of warp 1 issues the six MMAs of a chunk
-// as soon as the stage is full and commits them to the stage's "done"
-// mbarrier, after which the stage is refilled.  As many stages as fit in
-// shared memory (8 for 160 states, one CTA per SM).  The epilogue reads the
-// accumulator from tensor memory (one warp per 32 rows) and applies the
-// recurrence in FP32.
+//    (written by k_split3 before the launch) with 16-byte cp.async copies
+//    (L2 evict-last: rows are re-read by many tiles) into the row ring, in
+//    the MN-major operand layout with the 128-byte swizzle: 8 lanes read one
+//    whole 128-byte piece of a row, so one instruction moves four rows.
+// Warp roles (10 warps, one CTA per SM):
+//  - warp 0, one thread: the H copies, up to nh (8-12) chunks ahead;
+//  - warps 3-9: the row gathers, whole chunks in turn; a warp waits for its
+//    own copies and fences them for the async proxy before it arrives;
+//  - warp 2, one thread: waits for each chunk's "full" mbarrier in order and
+//    publishes the count of ready chunks in shared memory;
+//  - warp 1, one thread: six MMAs and one commit (to the chunk's "done"
+//    mbarrier) per chunk.  It never waits on an mbarrier itself: such a wait
+//    queues behind its outstanding MMAs (about 0.1 us per chunk).
+// Waits off the critical path back off with nanosleep: tight polling by many
+// threads slows every mbarrier operation of the CTA.  After the last chunk,
+// warps 0-3 (one per 32 TMEM lanes) read the accumulator from tensor memory
+// and apply the recurrence in FP32.
 // Every mbarrier wait is bounded; a wait that runs out sets an error word.
 
 #include <cuda_bf16.h>
@@ -53,13 +59,19 @@ constexpr int UK = 16;                        // slots per chunk (MMA K)
 constexpr int PLANE_ELEMS = UR * UK;          // 2048 BF16 = 4096 bytes
 constexpr int CHUNK_ELEMS = 3 * PLANE_ELEMS;  // three planes
 constexpr int CHUNK_BYTES = 2 * CHUNK_ELEMS;  // 12288
-constexpr int kMaxStages = 8;                // pipeline depth: as many as fit in shared memory
+constexpr int kMaxH = 12;                     // H ring stages (12 KB each)
+constexpr int kMaxB = 8;                      // gathered-row ring stages
 constexpr int kSmemBudget = 227 * 1024 - 1024;
 constexpr int kThreads = 320;                // 10 warps
-constexpr int kProducerWarps = 9;             // every warp but warp 1 loads (at most nst of them)
-constexpr int kMmaWarp = 1;                   // warp 1 issues the MMAs
+constexpr int kHWarp = 0;                     // lane 0 copies the H blocks
+constexpr int kMmaWarp = 1;                   // lane 0 issues the MMAs
+constexpr int kWaitWarp = 2;                  // waits for full stages on the MMA warp's behalf
+constexpr int kFirstBWarp = 3;                // warps 3-9 gather the block's rows
+constexpr int kBWarps = 7;
 constexpr int kMaxWait = 1 << 20;
 constexpr int kColAhead = 4;                  // chunks per warp whose column indices are loaded ahead
+constexpr int kAtom = 64;                     // states per 128-byte swizzle row
+constexpr int kAtomBytes = 16 * 128;          // one atom of a chunk: 16 slot rows x 128 bytes
 
 // Canonical no-swizzle layouts (8 x 16-byte core matrices, 128 bytes each):
 // core matrices 128 bytes apart along K and 256 bytes apart along M / N.
@@ -77,6 +89,19 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   d |= (uint64_t)(256 >> 4) << 32;        // stride byte offset: next core matrix along M/N
   d |= (uint64_t)1 << 46;                 // descriptor version
   return d;                               // base offset 0, no swizzle
+}
+
+// B operand (slots x states, states contiguous) in the 128-byte swizzle
+// layout: per 64-state atom 16 slot rows of 128 bytes, the 16-byte piece j of
+// row s stored at piece j ^ (s % 8); rows 8-15 1024 bytes after rows 0-7
+// (stride byte offset), atoms 2048 bytes apart (leading byte offset).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)(kAtomBytes >> 4) << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;                 // 128-byte swizzle
+  return d;
 }
 
 // kind::f16 instruction descriptor: BF16 x BF16 -> FP32, A K-major, B MN-major
@@ -103,10 +128,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
   return false;
 }
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src)
-               : "memory");
+// For waits off the critical path: a thread that polls an mbarrier without
+// pause slows the mbarrier operations of the threads that are on it.
+__device__ __forceinline__ bool mbar_wait_idle(uint64_t* b, uint32_t parity, int ns) {
+  for (int i = 0; i < kMaxWait; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    __nanosleep(ns);
+  }
+  return false;
 }
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
@@ -115,22 +153,33 @@ __device__ __forceinline__ void cp_async_wait() {
 
 __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     const int64_t* __restrict__ tptr, const int* __restrict__ tcol, const int* __restrict__ rowmap,
-    const int* __restrict__ order, const __nv_bfloat16* __restrict__ hpl, const __nv_bfloat16* __restrict__ xpl,
-    int64_t pstride, int ps, const float* __restrict__ src, const float* xold, float* dst,
-    int k, int64_t ld, float alpha, float beta, float delta,
-    uint32_t tmem_cols, int nst, int* __restrict__ err) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t full[kMaxStages];
-  __shared__ __align__(8) uint64_t mdone[kMaxStages];
+    const int* __restrict__ order, const __nv_bfloat16* __restrict__ hpl,
+    const __nv_bfloat16* __restrict__ xpl, int64_t pstride, int ps, const float* __restrict__ src,
+    const float* xold, float* dst, int k, int64_t ld, float alpha, float beta, float delta,
+    uint32_t tmem_cols, int nh, int nb, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // rings start on a 1024-byte boundary (swizzle atoms; descriptor base offset 0):
+  // nb gathered-row stages, then nh H stages
+  unsigned char* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+  // full[c % nd]: both stages of chunk c have landed (the H copy by bytes and
+  // an arrive each from the H and row producers); done[c % nd]: the MMAs of
+  // chunk c have read them.  nd >= nh, nb: a producer refilling for chunk c
+  // has waited for chunk c - nh or c - nb, so chunk c - nd's phase is over.
+  __shared__ __align__(8) uint64_t full[kMaxH], done[kMaxH];
   __shared__ __align__(8) uint64_t accf;     // all MMAs of the tile done (one phase)
   __shared__ uint32_t tmem_slot;
+  __shared__ uint32_t ready;                 // chunks whose two stages are full
   // tiles in decreasing chunk count, so the longest start first and the short
   // ones fill the tail of the launch
   const int tile = __ldg(order + blockIdx.x), tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int stage_bytes = CHUNK_BYTES + 96 * k;          // H planes + 3 block planes
+  const int natoms = (k + kAtom - 1) / kAtom;
+  const int bplane = natoms * kAtomBytes;               // one gathered plane
+  const int bstage = 3 * bplane;
+  unsigned char* hring = smem + nb * bstage;
   const int64_t c_first = tptr[tile] / UK;
   const int nch = (int)((tptr[tile + 1] - tptr[tile]) / UK);
   const int ngrp = k >> 3;
+  const int nd = max(nh, nb);
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -138,11 +187,12 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    for (int s = 0; s < nst; ++s) {
-      mbar_init(&full[s], 2);                    // the owning warp: H copy's expect_tx + rows fenced
-      mbar_init(&mdone[s], 1);                   // one tcgen05.commit
+    for (int s = 0; s < nd; ++s) {
+      mbar_init(&full[s], 2);                    // H expect_tx arrive + the rows' warp
+      mbar_init(&done[s], 1);                    // one tcgen05.commit
     }
     mbar_init(&accf, 1);
+    ready = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -151,24 +201,51 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
   const uint32_t tmem = tmem_slot;
   bool ok = true;
 
-  if (warp != kMmaWarp) {
-    // producers: warps 0, 2, 3, ... (pw = 0 .. np-1) take whole chunks in turn,
-    // chunk c to warp c % np.  Chunk c goes into stage c % nst once the MMAs of
-    // chunk c - nst have read it; np <= nst keeps every waiter within one phase
-    // of the stage's "done" barrier (a warp's previous chunk c - np waited for
-    // chunk c - np - nst >= c - 2 nst).  The owning warp arrives on the stage's
-    // "full" barrier once its row copies have landed and are fenced; the H
-    // block completes by byte count.  A warp waits for its own copies only:
-    // the np warps fill np stages at once.
-    const int np = min(kProducerWarps, nst);
-    const int pw = warp == 0 ? 0 : warp - 1;
+  if (warp == kHWarp) {
+    // H ring: one thread copies chunk c's H block into stage c % nh once the
+    // MMAs of chunk c - nh have read it, running up to nh chunks ahead of the
+    // MMAs (the H copies come from HBM and are the slowest to land)
+    if (lane == 0) {
+      uint64_t pol_stream;
+      asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol_stream));
+      for (int c = 0; c < nch; ++c) {
+        const int s = c % nh;
+        // one wait per two chunks: the MMAs complete in order, so chunk
+        // c + 1 - nh done means chunk c - nh is done too
+        if (c >= nh && ((c - nh) & 1) == 0) {
+          const int x = (c + 1 < nch ? c + 1 : c) - nh;
+          ok &= mbar_wait(&done[x % nd], (x / nd) & 1);
+        }
+        const uint32_t fb = smem_u32(&full[c % nd]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb),
+                     "r"(CHUNK_BYTES) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+            " [%0], [%1], %2, [%3], %4;"
+            ::"r"(smem_u32(hring + s * CHUNK_BYTES)), "l"(hpl + (c_first + c) * CHUNK_ELEMS),
+              "r"(CHUNK_BYTES), "r"(fb), "l"(pol_stream)
+            : "memory");
+      }
+    }
+  } else if (warp >= kFirstBWarp) {
+    // gathered rows: warps kFirstBWarp.. (pw = 0 .. np-1) take whole chunks in
+    // turn, chunk c to warp c % np, into stage c % nb once the MMAs of chunk
+    // c - nb have read it.  np <= nb keeps every wait within one phase of the
+    // stage's "free" barrier (a warp's previous chunk c - np waited for chunk
+    // c - np - nb >= c - 2 nb).  A warp waits for its own copies, fences them
+    // for the tensor core's (async-proxy) reads and arrives on the stage's
+    // "full" barrier; the np warps fill np stages at once.
+    const int np = min(kBWarps, nb);
+    const int pw = warp - kFirstBWarp;
     if (pw < np) {
-      const int lsl = lane & 15, lhalf = lane >> 4;
-      // lane = slot (16) x half (2) of a 32-byte sector: one instruction writes
-      // 512 contiguous bytes of shared memory
-      const __nv_bfloat16* xl = xpl + 8 * lhalf;
-      const uint32_t dl = (uint32_t)(lhalf * 256 + lsl * 16);
-      const int* colp = tcol + c_first * UK + lsl;
+      // lane = row of a quad (lane / 8) x 16-byte piece of a 128-byte row
+      // (lane % 8): one instruction reads four whole 128-byte rows and writes
+      // four 128-byte rows of shared memory (128-byte swizzle: piece j of
+      // slot row s lands at piece j ^ (s % 8))
+      const int lr = lane >> 3, lj = lane & 7;
+      uint64_t pol_keep;     // the block's rows are re-read by many tiles
+      asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol_keep));
+      const int* colp = tcol + c_first * UK + (lane & 15);
       // column indices of this warp's next kColAhead chunks live in registers
       int cur[kColAhead], nxt[kColAhead];
 #pragma unroll
@@ -186,35 +263,33 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
         for (int j = 0; j < kColAhead; ++j) {
           const int c = c0 + j * np;
           if (c >= nch) break;
-          const int s = c % nst;
-          if (c >= nst) ok &= mbar_wait(&mdone[s], ((c / nst) - 1) & 1);
-          unsigned char* st = smem + s * stage_bytes;
-          if (lane == 0) {
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                         ::"r"(smem_u32(&full[s])), "r"(CHUNK_BYTES) : "memory");
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                ::"r"(smem_u32(st)), "l"(hpl + (c_first + c) * CHUNK_ELEMS), "r"(CHUNK_BYTES),
-                "r"(smem_u32(&full[s]))
-                : "memory");
-          }
-          const __nv_bfloat16* xs = xl + (int64_t)cur[j] * ps;
-          const uint32_t d0 = smem_u32(st + CHUNK_BYTES) + dl;
+          const int s = c % nb;
+          if (c >= nb) ok &= mbar_wait_idle(&done[(c - nb) % nd], ((c - nb) / nd) & 1, 64);
+          const uint32_t sb = smem_u32(smem + s * bstage);
 #pragma unroll
-          for (int pl = 0; pl < 3; ++pl)
-            for (int g = 0; g < ngrp; g += 2)   // ngrp = k / 8 is even
-              asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
-                           ::"r"(d0 + (uint32_t)(pl * 32 * k + g * 256)), "l"(xs + pl * pstride + 8 * g)
-                           : "memory");
-          // the rows were written through the generic proxy: each thread waits
-          // for its own copies and fences them for the tensor core's
-          // (async-proxy) reads before the warp signals the stage
+          for (int rq = 0; rq < 4; ++rq) {
+            const int srow = 4 * rq + lr;                    // slot of this lane's row
+            const int64_t col = __shfl_sync(0xffffffffu, cur[j], srow);
+            const __nv_bfloat16* xs = xpl + col * ps + 8 * lj;
+            const uint32_t drow = sb + (uint32_t)((srow >> 3) * 1024 + (srow & 7) * 128 +
+                                                  ((lj ^ (srow & 7)) << 4));
+            for (int a = 0; a < natoms; ++a) {
+              if (a * 8 + lj < ngrp) {
+#pragma unroll
+                for (int pl = 0; pl < 3; ++pl)
+                  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;"
+                               ::"r"(drow + (uint32_t)(pl * bplane + a * kAtomBytes)),
+                                 "l"(xs + pl * pstride + a * kAtom), "l"(pol_keep)
+                               : "memory");
+              }
+            }
+          }
           cp_async_commit();
           cp_async_wait<0>();
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           __syncwarp();
           if (lane == 0)
-            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full[s]))
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full[c % nd]))
                          : "memory");
         }
 #pragma unroll
@@ -222,31 +297,60 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
       }
       cp_async_wait<0>();
     }
+  } else if (warp == kWaitWarp) {
+    // waits for each chunk's stages to fill, in order, and publishes the count of
+    // ready chunks to the MMA thread: an mbarrier wait by the MMA-issuing
+    // thread itself queues behind its outstanding MMAs (about 0.1 us a chunk)
+    if (lane == 0) {
+      for (int c = 0; c < nch; ++c) {
+        ok &= mbar_wait(&full[c % nd], (c / nd) & 1);
+        asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"(smem_u32(&ready)), "r"(c + 1)
+                     : "memory");
+      }
+    }
   } else if (lane == 0) {
-    // MMA issuer: six MMAs per chunk (term pairs, smallest products first)
+    // MMA thread: six MMAs per chunk (term pairs, smallest products first),
+    // committed to the chunk's "done" barrier.  Its per-chunk work is kept to
+    // a short dependency chain (stage addresses and descriptors advance by
+    // additions): the issue of the next chunk waits on it.
     const uint32_t idesc = instr_desc(UR, k);
-    const int pa[6] = {1, 0, 2, 0, 1, 0};
-    const int pb[6] = {1, 2, 0, 1, 0, 0};
+    const uint64_t da_hi = smem_desc(0), db_hi = smem_desc_sw128(0);
+    const uint32_t a_first = smem_u32(hring) >> 4, b_first = smem_u32(smem) >> 4;
+    const uint32_t a_end = a_first + nh * (CHUNK_BYTES >> 4);
+    const uint32_t b_end = b_first + nb * (bstage >> 4);
+    const uint32_t bpl = (uint32_t)bplane >> 4, apl = (2 * PLANE_ELEMS) >> 4;
+    const uint32_t done0 = smem_u32(&done[0]);
+    uint32_t a_lo = a_first, b_lo = b_first;
+    int sd = 0;
+    uint32_t avail = 0;
     for (int c = 0; c < nch; ++c) {
-      const int s = c % nst;
-      ok &= mbar_wait(&full[s], (c / nst) & 1);
+      for (int i = 0; i < kMaxWait && avail <= (uint32_t)c; ++i)
+        asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(avail) : "r"(smem_u32(&ready))
+                     : "memory");
+      ok &= avail > (uint32_t)c;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a0 = smem_u32(smem + s * stage_bytes);
-      const uint32_t b0 = a0 + CHUNK_BYTES;
+      // (term of A, term of B): (1,1) (0,2) (2,0) (0,1) (1,0) (0,0)
+      const uint64_t da[6] = {da_hi | (a_lo + apl), da_hi | a_lo, da_hi | (a_lo + 2 * apl),
+                              da_hi | a_lo, da_hi | (a_lo + apl), da_hi | a_lo};
+      const uint64_t db[6] = {db_hi | (b_lo + bpl), db_hi | (b_lo + 2 * bpl), db_hi | b_lo,
+                              db_hi | (b_lo + bpl), db_hi | b_lo, db_hi | b_lo};
 #pragma unroll
       for (int q = 0; q < 6; ++q) {
-        const uint64_t da = smem_desc(a0 + pa[q] * (2 * PLANE_ELEMS));
-        const uint64_t db = smem_desc(b0 + pb[q] * (32 * k));
         const uint32_t acc = (c > 0 || q > 0) ? 1u : 0u;
         asm volatile(
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-            ::"r"(tmem), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+            ::"r"(tmem), "l"(da[q]), "l"(db[q]), "r"(idesc), "r"(acc));
       }
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-          ::"r"(smem_u32(&mdone[s]))
+          ::"r"(done0 + 8 * sd)
           : "memory");
+      a_lo += CHUNK_BYTES >> 4;
+      if (a_lo == a_end) a_lo = a_first;
+      b_lo += bstage >> 4;
+      if (b_lo == b_end) b_lo = b_first;
+      if (++sd == nd) sd = 0;
     }
     if (nch > 0)
       asm volatile(
@@ -256,9 +360,9 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
   }
   __syncwarp();
   // all MMAs done.  A barrier of its own, used for one phase: a thread may
-  // get here long before the last chunk's stage barrier has passed the phase
-  // before its last one, where a parity wait on it would pass early.
-  if (nch > 0) ok &= mbar_wait(&accf, 0);
+  // get here long before the last chunk's stage barriers have passed the
+  // phase before their last one, where a parity wait on them would pass early.
+  if (nch > 0) ok &= mbar_wait_idle(&accf, 0, 512);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   // epilogue (warps 0-3, one per 32 TMEM lanes): row = warp*32 + lane of the
@@ -526,16 +630,21 @@ ttg_status launch_cheb_umma(ttg_op* op, const void* src, const void* xold, void*
   TTG_LAUNCHED(op);
   uint32_t cols = 32;
   while ((int)cols < k) cols <<= 1;
-  const int stage_bytes = CHUNK_BYTES + 96 * k;
-  const int nst = std::min(kMaxStages, kSmemBudget / stage_bytes);
-  if (nst < 3) return TTG_BAD_ARG;
-  const size_t smem = (size_t)nst * stage_bytes;
+  const int natoms = (k + kAtom - 1) / kAtom;
+  const int bstage = 3 * natoms * kAtomBytes;
+  // eight H stages (the H copies run ahead of the rows), the rest to the
+  // row stages, then what is left to more H stages (1024 bytes go to alignment)
+  const int avail = kSmemBudget - 1024;
+  const int nb = std::min(kMaxB, (avail - 8 * CHUNK_BYTES) / bstage);
+  const int nh = std::min(kMaxH, (avail - nb * bstage) / CHUNK_BYTES);
+  if (nb < 3 || nh < 3) return TTG_BAD_ARG;
+  const size_t smem = (size_t)nb * bstage + (size_t)nh * CHUNK_BYTES + 1024;
   k_cheb_umma<<<(unsigned)U.n_tiles, kThreads, smem, op->stream>>>(
       U.tptr.as<int64_t>(), U.tcol.as<int>(), U.rowmap.as<int>(), U.order.as<int>(),
-      U.hpl.as<__nv_bfloat16>(),
-      U.xpl.as<__nv_bfloat16>(), pstride, ps, reinterpret_cast<const float*>(src),
-      reinterpret_cast<const float*>(xold), reinterpret_cast<float*>(dst), k, op->ld,
-      (float)alpha, (float)beta, (float)delta, cols, nst, U.err.as<int>()); TTG_COUNT();
+      U.hpl.as<__nv_bfloat16>(), U.xpl.as<__nv_bfloat16>(), pstride, ps,
+      reinterpret_cast<const float*>(src), reinterpret_cast<const float*>(xold),
+      reinterpret_cast<float*>(dst), k, op->ld, (float)alpha, (float)beta, (float)delta, cols, nh,
+      nb, U.err.as<int>()); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
