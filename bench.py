@@ -45,11 +45,12 @@ METRIC = "s/SCF-iter & time-to-SCF @\u0394E<1e-5 Ha/atom: mixed+learned vs FP64,
 WORKLOAD = "atoms64"
 MIX_ALPHA = 0.1          # Anderson mixing parameter of this workload (input parameter)
 MIX_DEPTH = 10           # Anderson history (the reference example's history=10)
-# DRAM bytes per 64-row column slot of one FP32 filter degree, measured by
-# ncu on the 8-atom operator with a 160-column block (profile_workload
-# --workload atoms8 --states 160: 112.3 MB read + 3.7 MB written over 410,304
-# slots); scaled to the timed operator's slots
-TRAFFIC_PER_SLOT_FP32 = (112.280576e6 + 3.688448e6) / 410304
+# DRAM bytes per 128-row column slot of one FP32 filter degree (k_cheb_umma),
+# measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass) on
+# the 64-atom operator with its 160-column block (profile_workload --workload
+# atoms64 --prec fp32 --degrees 1): bytes / 3,760,928 slots; scaled to the
+# timed operator's slots
+TRAFFIC_PER_SLOT_UMMA = (3.63e9 + 40.42e6) / 3760928
 MAX_ITER = 60
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
@@ -204,6 +205,9 @@ def run_ours(args, rank, world):
     it = g.iterate(max_iter=args.warmup + args.steps, tol=0.0)
     for _ in range(args.warmup):
         next(it)
+    # every fused filter-degree launch of the timed iterations bracketed by
+    # CUDA events on the operator's stream
+    g.op.kernel_timing(True)
     barrier(world)
     clocks = Clocks()
     clocks.start()
@@ -221,33 +225,26 @@ def run_ours(args, rank, world):
             phases[key] = phases.get(key, 0.0) + v * 1e3 / args.steps
     passes = float(np.mean([r["passes"] for r in recs]))
 
-    # ---- dominant kernel: one FP32 filter degree (fused tensor-core SpMM +
-    # recurrence) and one BF16 degree, on the operator of the last iteration
+    # ---- dominant kernel: the FP32 filter degree (tcgen05 SpMM fused with the
+    # recurrence), device time of its launches in the timed iterations
     op = g.op
     info = op.info()
     nnz = info["nnz_h"] + 2 * info["nnz_c"]
     n = s.N
-    X = g.X
-    w = g.eigenvalues
-    a, b, a0 = float(w[-1]), float(g.upper_bound), float(w[0])
-    ax = api.AX(1, k)
-    ax.op = op
-    roof = {}
     peak, peak_kind = peaks()
-    for prec, vsz in (("fp32", 4), ("bf16", 2)):
-        sch = api.sched(prec)
-        for _ in range(2):
-            api.ChebyShevFilter(sch).computeFilteredSubspace(None, ax, X, n, m, a, b, a0)
-        reps = 3
-        with Timer() as tf:
-            for _ in range(reps):
-                api.ChebyShevFilter(sch).computeFilteredSubspace(None, ax, X, n, m, a, b, a0)
-        per_deg = tf.s / reps / m
+    roof = {}
+    for kind, vsz in (("umma_fp32", 4), ("tc_fp32", 4), ("tc_bf16", 2)):
+        ms, cnt = op.kernel_time(kind)
+        if cnt == 0:
+            continue
+        per = ms / cnt / 1e3
+        # algorithmic bytes of one degree: H in CSR form at the degree's value
+        # width (value + int32 column per nonzero, row pointers), Y read, X read,
+        # Ynew written
         bytes_deg = nnz * (vsz + 4) + 4 * (n + 1) + 3 * n * k * vsz
-        roof[prec] = {"launch_ms": per_deg * 1e3, "bytes_per_launch": bytes_deg,
-                      "flops_per_launch": 2.0 * nnz * k, "achieved": bytes_deg / per_deg / 1e9}
-    api.MultTM().orth(X)
-    del X, ax
+        roof[kind] = {"launch_ms": per * 1e3, "launches": cnt, "bytes_per_launch": bytes_deg,
+                      "flops_per_launch": 2.0 * nnz * k, "achieved": bytes_deg / per / 1e9}
+    op.kernel_timing(False)
     g.close()
     del g, it
 
@@ -289,7 +286,11 @@ def run_ours(args, rank, world):
     cpu = (cpu_baseline(s, passes, rho_host, None)
            if (rank == 0 and world == 1 and not args.no_cpu) else None)
     if rank == 0:
-        r32 = roof["fp32"]
+        r32 = roof.get("umma_fp32") or roof["tc_fp32"]
+        kname = ("k_cheb_umma (one FP32 filter degree: tcgen05 SpMM, three-term BF16 "
+                 "split, fused with the recurrence)" if "umma_fp32" in roof else
+                 "k_cheb_tc<float, 5> (one FP32 filter degree: 3xTF32 mma.sync SpMM fused "
+                 "with the recurrence)")
         line = {
             "metric": METRIC, "value": sec_per_iter, "unit": "s/SCF-iter", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_iter * 1e3,
@@ -305,20 +306,26 @@ def run_ours(args, rank, world):
                              "fields of 373 MB" % (info["device_bytes"] / 1e9),
                        "parallelism": f"replicas x{world}", "system_gen_s": round(gen_s, 1)},
             "time_to_scf": tts,
-            "roofline": {"bound": "hbm", "kernel": "k_cheb_tc<float, 5> (one FP32 filter "
-                         "degree: 3xTF32 tensor-core SpMM fused with the recurrence)",
+            "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": r32["achieved"], "peak": peak,
                          "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s",
                          "frac": r32["achieved"] / peak,
-                         "traffic": TRAFFIC_PER_SLOT_FP32 * info["tile_slots"],
-                         "traffic_note": "ncu DRAM bytes per slot of the 8-atom capture x this "
-                                         "operator's tile slots",
+                         "traffic": (TRAFFIC_PER_SLOT_UMMA * info["umma_slots"]
+                                     if "umma_fp32" in roof else None),
+                         "traffic_note": "ncu DRAM bytes per 128-row slot of one k_cheb_umma "
+                                         "launch on this workload x this operator's slots",
+                         "timing": "CUDA events around every launch of the kernel on the "
+                                   "operator's stream during the timed iterations",
+                         "launches": r32["launches"],
                          "bytes_per_launch": r32["bytes_per_launch"],
                          "flops_per_launch": r32["flops_per_launch"],
                          "launch_ms": r32["launch_ms"]},
-            "roofline_bf16_degree": {"achieved": roof["bf16"]["achieved"], "unit": "GB/s",
-                                     "frac": roof["bf16"]["achieved"] / peak,
-                                     "launch_ms": roof["bf16"]["launch_ms"]},
+            "roofline_bf16_degree": ({"kernel": "k_cheb_tc<bf16, 5>",
+                                      "achieved": roof["tc_bf16"]["achieved"], "unit": "GB/s",
+                                      "frac": roof["tc_bf16"]["achieved"] / peak,
+                                      "launch_ms": roof["tc_bf16"]["launch_ms"],
+                                      "launches": roof["tc_bf16"]["launches"]}
+                                     if "tc_bf16" in roof else None),
             "e2e": {"value": e2e, "unit": "s/SCF-iter", "h2d_bytes_per_step": int(nq * 8),
                     "d2h_bytes_per_step": int(2 * nq * 8 + p3 * k * 8),
                     "what": "same iterations with rho_in and rho_out passing through pinned "
@@ -327,6 +334,7 @@ def run_ours(args, rank, world):
             "gpu_launches_per_step": launches / args.steps,
             "phases_ms": {k_: round(v, 2) for k_, v in phases.items()},
             "tile_fill": info["tile_fill"],
+            "umma_tile_fill": (info["nnz_h"] + info["nnz_c"]) / max(1, 128 * info["umma_slots"]),
             "clocks": ck,
             "cpu_baseline": cpu,
         }

@@ -127,6 +127,20 @@ ttg_status ttg_op_sync(ttg_op* op);
 ttg_status ttg_op_record(ttg_op* op, int32_t slot);
 ttg_status ttg_op_elapsed_ms(ttg_op* op, int32_t slot0, int32_t slot1, float* ms);
 
+/* Device time of the fused filter-degree kernels (one launch per degree), by
+ * kind.  With timing on, each launch of such a kernel is bracketed by two
+ * CUDA events on the operator's stream; the pairs are read back in batches
+ * (no host wait per launch).  ttg_op_kernel_time synchronises the stream and
+ * returns the total milliseconds and the launch count of one kind since
+ * timing was switched on; enable = 0 switches it off and clears the totals. */
+#define TTG_KT_UMMA_FP32 0   /* tcgen05 FP32 degree (three-term BF16 split) */
+#define TTG_KT_TC_FP32 1     /* mma.sync FP32 degree (3xTF32) */
+#define TTG_KT_TC_BF16 2     /* mma.sync BF16 degree */
+#define TTG_KT_ROWGROUP 3    /* CUDA-core row-group degree (any precision) */
+#define TTG_KT_KINDS 4
+ttg_status ttg_op_kernel_timing(ttg_op* op, int32_t enable);
+ttg_status ttg_op_kernel_time(ttg_op* op, int32_t kind, double* ms_total, int64_t* launches);
+
 /* ---- vector blocks (the reference's dense Mat X, N x k) ----------------- */
 
 ttg_status ttg_block_create(ttg_op* op, int32_t k, ttg_block** out);

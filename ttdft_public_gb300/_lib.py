@@ -65,6 +65,8 @@ _SIGS = {
     "ttg_op_sync": [c_vp],
     "ttg_op_record": [c_vp, c_i32],
     "ttg_op_elapsed_ms": [c_vp, c_i32, c_i32, c_vp],
+    "ttg_op_kernel_timing": [c_vp, c_i32],
+    "ttg_op_kernel_time": [c_vp, c_i32, c_vp, c_vp],
     "ttg_block_create": [c_vp, c_i32, c_vp],
     "ttg_block_destroy": [c_vp],
     "ttg_block_set": [c_vp, c_vp, c_i64],

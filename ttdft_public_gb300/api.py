@@ -112,6 +112,22 @@ class Operator:
         check(_lib.ttg().ttg_op_elapsed_ms(self.h, s0, s1, ctypes.byref(ms)), "ttg_op_elapsed_ms")
         return ms.value
 
+    # kinds of ttg_op_kernel_time (include/ttg.h TTG_KT_*)
+    KERNEL_KINDS = {"umma_fp32": 0, "tc_fp32": 1, "tc_bf16": 2, "rowgroup": 3}
+
+    def kernel_timing(self, enable: bool):
+        """Bracket every fused filter-degree launch with CUDA events on the
+        operator's stream (off: stop and clear the totals)."""
+        check(_lib.ttg().ttg_op_kernel_timing(self.h, 1 if enable else 0), "ttg_op_kernel_timing")
+
+    def kernel_time(self, kind: str):
+        """(total device milliseconds, launches) of one kernel kind since
+        timing was switched on."""
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        check(_lib.ttg().ttg_op_kernel_time(self.h, self.KERNEL_KINDS[kind], ctypes.byref(ms),
+                                            ctypes.byref(n)), "ttg_op_kernel_time")
+        return ms.value, n.value
+
     def stream(self) -> int:
         return _lib.ttg().ttg_op_stream(self.h)
 

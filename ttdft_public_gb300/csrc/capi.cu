@@ -50,6 +50,41 @@ namespace ttg {
 std::atomic<long long> g_kernel_launches{0};
 }
 
+namespace ttg {
+
+static ttg_status kt_flush(ttg_op* op) {
+  KernelTimer& T = op->kt;
+  if (T.used == 0) return TTG_OK;
+  TTG_CUDA_TRY(cudaEventSynchronize(T.ev[2 * T.used - 1]));
+  for (int i = 0; i < T.used; ++i) {
+    float ms = 0.f;
+    TTG_CUDA_TRY(cudaEventElapsedTime(&ms, T.ev[2 * i], T.ev[2 * i + 1]));
+    T.ms[T.kind[i]] += ms;
+    T.count[T.kind[i]]++;
+  }
+  T.used = 0;
+  return TTG_OK;
+}
+
+ttg_status kt_begin(ttg_op* op, int kind) {
+  KernelTimer& T = op->kt;
+  if (!T.on) return TTG_OK;
+  if (T.used == KernelTimer::kPairs) TTG_TRY(kt_flush(op));
+  T.kind[T.used] = kind;
+  TTG_CUDA_TRY(cudaEventRecord(T.ev[2 * T.used], op->stream));
+  return TTG_OK;
+}
+
+ttg_status kt_end(ttg_op* op) {
+  KernelTimer& T = op->kt;
+  if (!T.on) return TTG_OK;
+  TTG_CUDA_TRY(cudaEventRecord(T.ev[2 * T.used + 1], op->stream));
+  T.used++;
+  return TTG_OK;
+}
+
+}  // namespace ttg
+
 extern "C" {
 
 const char* ttg_version(void) { return "ttg 0.1 (sm_103a)"; }
@@ -168,8 +203,39 @@ ttg_status ttg_op_destroy(ttg_op* op) {
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < kMaxSlots; ++i)
     if (op->ev[i]) cudaEventDestroy(op->ev[i]);
+  for (cudaEvent_t e : op->kt.ev)
+    if (e) cudaEventDestroy(e);
   if (op->stream) cudaStreamDestroy(op->stream);
   delete op;
+  return TTG_OK;
+}
+
+ttg_status ttg_op_kernel_timing(ttg_op* op, int32_t enable) {
+  if (!op) return TTG_BAD_ARG;
+  KernelTimer& T = op->kt;
+  if (enable && !T.on) {
+    if (T.ev.empty()) {
+      T.ev.resize(2 * KernelTimer::kPairs, nullptr);
+      T.kind.resize(KernelTimer::kPairs, 0);
+      for (cudaEvent_t& e : T.ev) TTG_CUDA_TRY(cudaEventCreate(&e));
+    }
+    T.on = true;
+  } else if (!enable) {
+    if (T.on) TTG_TRY(kt_flush(op));
+    T.on = false;
+    for (int i = 0; i < TTG_KT_KINDS; ++i) {
+      T.ms[i] = 0.0;
+      T.count[i] = 0;
+    }
+  }
+  return TTG_OK;
+}
+
+ttg_status ttg_op_kernel_time(ttg_op* op, int32_t kind, double* ms_total, int64_t* launches) {
+  if (!op || kind < 0 || kind >= TTG_KT_KINDS || !ms_total || !launches) return TTG_BAD_ARG;
+  TTG_TRY(kt_flush(op));
+  *ms_total = op->kt.ms[kind];
+  *launches = op->kt.count[kind];
   return TTG_OK;
 }
 

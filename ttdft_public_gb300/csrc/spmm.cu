@@ -681,11 +681,13 @@ static ttg_status launch_step_t(ttg_op* op, const TV* vals, const void* src, con
   threads = (threads + 31) / 32 * 32;
   if (threads > 512) return TTG_BAD_ARG;
   if (op->rg.n_groups == 0) return TTG_OK;
+  TTG_TRY(kt_begin(op, TTG_KT_ROWGROUP));
   k_cheb_step<TV, TS, TA, G, VEC, CH><<<(unsigned)op->rg.n_groups, threads, 0, op->stream>>>(
       op->rg.gptr.as<int64_t>(), op->rg.gcol.as<int>(), vals,
       reinterpret_cast<const TS*>(src), reinterpret_cast<const TS*>(xold),
       reinterpret_cast<TS*>(dst), op->n, k, op->ld, (TA)alpha, (TA)beta, (TA)delta); TTG_COUNT();
   TTG_LAUNCHED(op);
+  TTG_TRY(kt_end(op));
   return TTG_OK;
 }
 

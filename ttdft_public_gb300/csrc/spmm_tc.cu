@@ -31,6 +31,8 @@
 #include <omp.h>
 #endif
 
+#include <type_traits>
+
 #include "ttg_internal.cuh"
 
 namespace ttg {
@@ -417,12 +419,14 @@ static ttg_status launch_tc_t(ttg_op* op, const void* hval, const void* src, con
                               void* dst, int k, double alpha, double beta, double delta) {
   constexpr int KS = 32 * MT;
   dim3 grid((unsigned)op->tiles.n_tiles, (unsigned)((k + KS - 1) / KS));
+  TTG_TRY(kt_begin(op, std::is_same<T, float>::value ? TTG_KT_TC_FP32 : TTG_KT_TC_BF16));
   k_cheb_tc<T, MT><<<grid, 128, 0, op->stream>>>(
       op->tiles.tptr.as<int64_t>(), op->tiles.tcol.as<int>(), op->tiles.rowmap.as<int>(),
       reinterpret_cast<const typename TcTraits<T>::HV*>(hval), reinterpret_cast<const T*>(src),
       reinterpret_cast<const T*>(xold), reinterpret_cast<T*>(dst), k, op->ld, (float)alpha,
       (float)beta, (float)delta); TTG_COUNT();
   TTG_LAUNCHED(op);
+  TTG_TRY(kt_end(op));
   return TTG_OK;
 }
 

@@ -639,6 +639,7 @@ ttg_status launch_cheb_umma(ttg_op* op, const void* src, const void* xold, void*
   const int nh = std::min(kMaxH, (avail - nb * bstage) / CHUNK_BYTES);
   if (nb < 3 || nh < 3) return TTG_BAD_ARG;
   const size_t smem = (size_t)nb * bstage + (size_t)nh * CHUNK_BYTES + 1024;
+  TTG_TRY(kt_begin(op, TTG_KT_UMMA_FP32));
   k_cheb_umma<<<(unsigned)U.n_tiles, kThreads, smem, op->stream>>>(
       U.tptr.as<int64_t>(), U.tcol.as<int>(), U.rowmap.as<int>(), U.order.as<int>(),
       U.hpl.as<__nv_bfloat16>(), U.xpl.as<__nv_bfloat16>(), pstride, ps,
@@ -646,6 +647,7 @@ ttg_status launch_cheb_umma(ttg_op* op, const void* src, const void* xold, void*
       reinterpret_cast<float*>(dst), k, op->ld, (float)alpha, (float)beta, (float)delta, cols, nh,
       nb, U.err.as<int>()); TTG_COUNT();
   TTG_LAUNCHED(op);
+  TTG_TRY(kt_end(op));
   return TTG_OK;
 }
 

@@ -143,6 +143,19 @@ struct Pattern {
   DevBuf work2;
 };
 
+// Device time of the fused filter-degree kernels, by kind (TTG_KT_*): with
+// timing on, each such launch is bracketed by two events on the operator's
+// stream; pairs are read back in batches, so timing never waits on the host.
+struct KernelTimer {
+  static constexpr int kPairs = 1024;
+  bool on = false;
+  std::vector<cudaEvent_t> ev;   // 2 * kPairs
+  std::vector<int> kind;         // kind of each pending pair
+  int used = 0;
+  double ms[TTG_KT_KINDS] = {};
+  long long count[TTG_KT_KINDS] = {};
+};
+
 struct Csr {
   int64_t rows = 0, cols = 0, nnz = 0, max_row_nnz = 0;
   DevBuf ptr;      // int64
@@ -184,6 +197,7 @@ struct ttg_op {
   ttg::DevBuf scal;           // small FP64 scratch (reductions, status)
   ttg::DevBuf status;         // int32 device status words
   cudaEvent_t ev[ttg::kMaxSlots] = {};
+  ttg::KernelTimer kt;
   int64_t launches = 0;
   int64_t device_bytes = 0;
 };
@@ -195,6 +209,10 @@ struct ttg_block {
 };
 
 namespace ttg {
+
+// capi.cu: kernel timer (no-ops while timing is off)
+ttg_status kt_begin(ttg_op* op, int kind);
+ttg_status kt_end(ttg_op* op);
 
 // spmm.cu
 ttg_status build_row_groups(ttg_op* op, int64_t n, const int64_t* hp, const int32_t* hc,
