@@ -22,8 +22,9 @@
 //                          computeRhoIn (dft/AndersonMixing.cc:267-316).
 //
 // Fields are x-fastest n1 x n2 x n3 arrays in device memory owned by the
-// caller.  The mode products and Gram matrices are one FP64 strided-batched
-// GEMM kernel with a fixed-order split-K reduction (bitwise reproducible).
+// caller.  The mode products and Gram matrices are one strided-batched GEMM
+// kernel (FP64 in and out, double-FP32 arithmetic on the FP32 pipe) with a
+// fixed-order split-K reduction in FP64 (bitwise reproducible).
 
 #include <algorithm>
 #include <cmath>
@@ -38,15 +39,44 @@ namespace {
 constexpr int DM = 64, DN = 64, DK = 16;
 constexpr int64_t kNumSMs = 152;
 
-// C[z] (+)= A[z] B[z] over a K range; split s of z_total = batch*splits writes
-// its partial to part + s*... when part != nullptr.
+// Double-FP32 ("df64") arithmetic: a value is an unevaluated sum hi + lo of
+// two floats (about 48 significant bits).  FP64 runs at ~1.25 TFLOP/s on
+// this part and FP32 at ~80, so the FP64 GEMMs run on the FP32 pipe in df64:
+// one df64 multiply-add is ~15 FP32 instructions (Dekker/Knuth error-free
+// product and sum), about 4x the FP64 rate.  The product's lo x lo term
+// (2^-48 relative) is dropped.
+struct F2 {
+  float h, l;
+};
+
+__device__ __forceinline__ F2 to_f2(double x) {
+  const float h = (float)x;
+  return F2{h, (float)(x - (double)h)};
+}
+
+// acc += a * b
+__device__ __forceinline__ void f2_fma(F2& acc, F2 a, F2 b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);          // exact: a.h b.h = p + e
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float s = acc.h + p;             // two-sum of the high parts
+  const float v = s - acc.h;
+  float t = (acc.h - (s - v)) + (p - v);
+  t += acc.l + e;
+  acc.h = s + t;                          // renormalise
+  acc.l = t - (acc.h - s);
+}
+
+// C[z] (+)= A[z] B[z] over a K range, in df64; split s of z_total =
+// batch*splits writes its partial to part + s*... when part != nullptr.
 // sym: the product is symmetric (a Gram matrix); tiles strictly above the
 // diagonal are skipped and filled by k_mirror_upper afterwards.
 __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, int splits, DOp A, DOp B,
                                                double* C, int64_t c_rs, int64_t c_cs, int64_t c_bs,
                                                double* part, int sym) {
-  __shared__ double sA[DK][DM + 1];
-  __shared__ double sB[DK][DN + 1];
+  __shared__ float sAh[DK][DM + 1], sAl[DK][DM + 1];
+  __shared__ float sBh[DK][DN + 1], sBl[DK][DN + 1];
   const int zz = blockIdx.z;
   const int z = zz / splits, sp = zz % splits;
   const int kchunk = (K + splits - 1) / splits;
@@ -64,31 +94,39 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, int splits, 
   const double* Bb = B.p + (int64_t)z * B.bs;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   const bool a_mfast = (A.rs == 1), b_nfast = (B.cs == 1);
-  double acc[4][4] = {};
+  F2 acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = F2{0.f, 0.f};
   for (int kb = kbeg; kb < kend; kb += DK) {
     for (int e = threadIdx.x; e < DK * DM; e += 256) {
       int mm, kk;
       if (a_mfast) { mm = e % DM; kk = e / DM; } else { kk = e % DK; mm = e / DK; }
       const int gm = m0 + mm, gk = kb + kk;
-      sA[kk][mm] = (gm < M && gk < kend) ? Ab[(int64_t)gm * A.rs + (int64_t)gk * A.cs] : 0.0;
+      const F2 av = to_f2((gm < M && gk < kend) ? Ab[(int64_t)gm * A.rs + (int64_t)gk * A.cs] : 0.0);
+      sAh[kk][mm] = av.h;
+      sAl[kk][mm] = av.l;
       int nn, kk2;
       if (b_nfast) { nn = e % DN; kk2 = e / DN; } else { kk2 = e % DK; nn = e / DK; }
       const int gn = n0 + nn, gk2 = kb + kk2;
-      sB[kk2][nn] = (gn < N && gk2 < kend) ? Bb[(int64_t)gk2 * B.rs + (int64_t)gn * B.cs] : 0.0;
+      const F2 bv = to_f2((gn < N && gk2 < kend) ? Bb[(int64_t)gk2 * B.rs + (int64_t)gn * B.cs] : 0.0);
+      sBh[kk2][nn] = bv.h;
+      sBl[kk2][nn] = bv.l;
     }
     __syncthreads();
-#pragma unroll
+#pragma unroll 4
     for (int t = 0; t < DK; ++t) {
-      double a[4], b[4];
+      F2 a[4], b[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        a[u] = sA[t][ty + 16 * u];
-        b[u] = sB[t][tx + 16 * u];
+        a[u] = F2{sAh[t][ty + 16 * u], sAl[t][ty + 16 * u]};
+        b[u] = F2{sBh[t][tx + 16 * u], sBl[t][tx + 16 * u]};
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        for (int v = 0; v < 4; ++v) f2_fma(acc[u][v], a[u], b[v]);
     }
     __syncthreads();
   }
@@ -98,8 +136,9 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, int splits, 
     for (int v = 0; v < 4; ++v) {
       const int m = m0 + ty + 16 * u, n = n0 + tx + 16 * v;
       if (m >= M || n >= N) continue;
-      if (part) part[((int64_t)zz * M + m) * N + n] = acc[u][v];
-      else C[(int64_t)z * c_bs + (int64_t)m * c_rs + (int64_t)n * c_cs] = acc[u][v];
+      const double r = (double)acc[u][v].h + (double)acc[u][v].l;
+      if (part) part[((int64_t)zz * M + m) * N + n] = r;
+      else C[(int64_t)z * c_bs + (int64_t)m * c_rs + (int64_t)n * c_cs] = r;
     }
 }
 
