@@ -20,7 +20,10 @@
 //                  (dft/KSDFTEnergyFunctional.cc:76-124) and occupations
 //                  (main.cc:1239-1272).
 //
-// FP64 throughout: these are the quantities the method keeps in double.
+// FP64 throughout: these are the quantities the method keeps in double.  The
+// two N x k GEMMs (the Gram X^T Y and the rotation X Q) read and write FP64
+// and compute in double-FP32 on the FP32 pipe (about 48 bits; FP64 runs at
+// a small fraction of the FP32 rate on this part).
 
 #include <algorithm>
 #include <cmath>
@@ -37,33 +40,41 @@ __global__ void __launch_bounds__(256) k_gram_tn(const double* __restrict__ X,
                                                  const double* __restrict__ Y, int64_t n,
                                                  int k, int64_t ld, int64_t rows_per_split,
                                                  double* __restrict__ part) {
-  __shared__ double sX[TK][TM + 1];
-  __shared__ double sY[TK][TN + 1];
+  __shared__ float sXh[TK][TM + 1], sXl[TK][TM + 1];
+  __shared__ float sYh[TK][TN + 1], sYl[TK][TN + 1];
   const int p0 = blockIdx.x * TM, q0 = blockIdx.y * TN;
   const int64_t r0 = (int64_t)blockIdx.z * rows_per_split;
   const int64_t r1 = (n < r0 + rows_per_split ? n : r0 + rows_per_split);
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  double acc[4][4] = {};
+  F2 acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = F2{0.f, 0.f};
   for (int64_t rb = r0; rb < r1; rb += TK) {
     for (int i = threadIdx.x; i < TK * TM; i += 256) {
       const int rr = i / TM, cc = i % TM;
       const int64_t row = rb + rr;
-      sX[rr][cc] = (row < r1 && p0 + cc < k) ? X[row * ld + p0 + cc] : 0.0;
-      sY[rr][cc] = (row < r1 && q0 + cc < k) ? Y[row * ld + q0 + cc] : 0.0;
+      const F2 xv = to_f2((row < r1 && p0 + cc < k) ? X[row * ld + p0 + cc] : 0.0);
+      const F2 yv = to_f2((row < r1 && q0 + cc < k) ? Y[row * ld + q0 + cc] : 0.0);
+      sXh[rr][cc] = xv.h;
+      sXl[rr][cc] = xv.l;
+      sYh[rr][cc] = yv.h;
+      sYl[rr][cc] = yv.l;
     }
     __syncthreads();
-#pragma unroll
+#pragma unroll 4
     for (int t = 0; t < TK; ++t) {
-      double a[4], b[4];
+      F2 a[4], b[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        a[u] = sX[t][ty + 16 * u];
-        b[u] = sY[t][tx + 16 * u];
+        a[u] = F2{sXh[t][ty + 16 * u], sXl[t][ty + 16 * u]};
+        b[u] = F2{sYh[t][tx + 16 * u], sYl[t][tx + 16 * u]};
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        for (int v = 0; v < 4; ++v) f2_fma(acc[u][v], a[u], b[v]);
     }
     __syncthreads();
   }
@@ -73,7 +84,8 @@ __global__ void __launch_bounds__(256) k_gram_tn(const double* __restrict__ X,
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       const int p = p0 + ty + 16 * u, q = q0 + tx + 16 * v;
-      if (p < k && q < k) out[p + (int64_t)q * k] = acc[u][v];   // column-major
+      if (p < k && q < k)     // column-major
+        out[p + (int64_t)q * k] = (double)acc[u][v].h + (double)acc[u][v].l;
     }
 }
 
@@ -92,38 +104,46 @@ __global__ void __launch_bounds__(256) k_gemm_nn(const double* __restrict__ X,
                                                  const double* __restrict__ Q,
                                                  double* __restrict__ out, int64_t n, int k,
                                                  int64_t ld, int transQ) {
-  __shared__ double sX[TM][TK + 1];
-  __shared__ double sQ[TK][TN + 1];
+  __shared__ float sXh[TM][TK + 1], sXl[TM][TK + 1];
+  __shared__ float sQh[TK][TN + 1], sQl[TK][TN + 1];
   const int64_t i0 = (int64_t)blockIdx.x * TM;
   const int q0 = blockIdx.y * TN;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  double acc[4][4] = {};
+  F2 acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = F2{0.f, 0.f};
   for (int pb = 0; pb < k; pb += TK) {
     for (int e = threadIdx.x; e < TM * TK; e += 256) {
       const int rr = e / TK, cc = e % TK;
       const int64_t row = i0 + rr;
-      sX[rr][cc] = (row < n && pb + cc < k) ? X[row * ld + pb + cc] : 0.0;
+      const F2 xv = to_f2((row < n && pb + cc < k) ? X[row * ld + pb + cc] : 0.0);
+      sXh[rr][cc] = xv.h;
+      sXl[rr][cc] = xv.l;
     }
     for (int e = threadIdx.x; e < TK * TN; e += 256) {
       const int rr = e / TN, cc = e % TN;
       const int p = pb + rr, q = q0 + cc;
       double v = 0.0;
       if (p < k && q < k) v = transQ ? Q[q + (int64_t)p * k] : Q[p + (int64_t)q * k];
-      sQ[rr][cc] = v;
+      const F2 qv = to_f2(v);
+      sQh[rr][cc] = qv.h;
+      sQl[rr][cc] = qv.l;
     }
     __syncthreads();
-#pragma unroll
+#pragma unroll 4
     for (int t = 0; t < TK; ++t) {
-      double a[4], b[4];
+      F2 a[4], b[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        a[u] = sX[ty + 16 * u][t];
-        b[u] = sQ[t][tx + 16 * u];
+        a[u] = F2{sXh[ty + 16 * u][t], sXl[ty + 16 * u][t]};
+        b[u] = F2{sQh[t][tx + 16 * u], sQl[t][tx + 16 * u]};
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        for (int v = 0; v < 4; ++v) f2_fma(acc[u][v], a[u], b[v]);
     }
     __syncthreads();
   }
@@ -133,7 +153,7 @@ __global__ void __launch_bounds__(256) k_gemm_nn(const double* __restrict__ X,
     for (int v = 0; v < 4; ++v) {
       const int64_t i = i0 + ty + 16 * u;
       const int q = q0 + tx + 16 * v;
-      if (i < n && q < k) out[i * ld + q] = acc[u][v];
+      if (i < n && q < k) out[i * ld + q] = (double)acc[u][v].h + (double)acc[u][v].l;
     }
 }
 

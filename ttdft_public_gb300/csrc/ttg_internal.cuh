@@ -242,6 +242,38 @@ ttg_status launch_convert(ttg_op* op, int from, int to, const void* src, void* d
                           int64_t rows, int k);
 
 // scf.cu: FP64 strided-batched GEMM (split-K when the output is small)
+#ifdef __CUDACC__
+// Double-FP32 ("df64") arithmetic: a value is an unevaluated sum hi + lo of
+// two floats (about 48 significant bits).  FP64 runs at ~1.25 TFLOP/s on
+// this part and FP32 at ~80, so the FP64 GEMMs run on the FP32 pipe in df64:
+// one df64 multiply-add is ~15 FP32 instructions (Dekker/Knuth error-free
+// product and sum), about 4x the FP64 rate.  The product's lo x lo term
+// (2^-48 relative) is dropped.
+struct F2 {
+  float h, l;
+};
+
+__device__ __forceinline__ F2 to_f2(double x) {
+  const float h = (float)x;
+  return F2{h, (float)(x - (double)h)};
+}
+
+// acc += a * b
+__device__ __forceinline__ void f2_fma(F2& acc, F2 a, F2 b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);          // exact: a.h b.h = p + e
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float s = acc.h + p;             // two-sum of the high parts
+  const float v = s - acc.h;
+  float t = (acc.h - (s - v)) + (p - v);
+  t += acc.l + e;
+  acc.h = s + t;                          // renormalise
+  acc.l = t - (acc.h - s);
+}
+
+#endif
+
 struct DOp {
   const double* p;
   int64_t rs, cs, bs;   // element strides: row (m or k), column (k or n), batch
