@@ -246,8 +246,8 @@ ttg_status launch_convert(ttg_op* op, int from, int to, const void* src, void* d
 // Double-FP32 ("df64") arithmetic: a value is an unevaluated sum hi + lo of
 // two floats (about 48 significant bits).  FP64 runs at ~1.25 TFLOP/s on
 // this part and FP32 at ~80, so the FP64 GEMMs run on the FP32 pipe in df64:
-// one df64 multiply-add is ~15 FP32 instructions (Dekker/Knuth error-free
-// product and sum), about 4x the FP64 rate.  The product's lo x lo term
+// one df64 multiply-add is 11 FP32 instructions (Dekker/Knuth error-free
+// product and sum), about 5x the FP64 rate.  The product's lo x lo term
 // (2^-48 relative) is dropped.
 struct F2 {
   float h, l;
@@ -258,7 +258,11 @@ __device__ __forceinline__ F2 to_f2(double x) {
   return F2{h, (float)(x - (double)h)};
 }
 
-// acc += a * b
+// acc += a * b.  The accumulator is left unnormalised (lo is not folded
+// into hi after every step): the loop-carried dependency is then a single
+// FP32 add on hi and one on lo, and the sum is read out as (double)hi +
+// (double)lo.  Over K terms lo collects at most K half-ulps of hi, so the
+// result keeps ~2^-47 relative accuracy for K up to ~2^20.
 __device__ __forceinline__ void f2_fma(F2& acc, F2 a, F2 b) {
   const float p = a.h * b.h;
   float e = fmaf(a.h, b.h, -p);          // exact: a.h b.h = p + e
@@ -266,10 +270,9 @@ __device__ __forceinline__ void f2_fma(F2& acc, F2 a, F2 b) {
   e = fmaf(a.l, b.h, e);
   const float s = acc.h + p;             // two-sum of the high parts
   const float v = s - acc.h;
-  float t = (acc.h - (s - v)) + (p - v);
-  t += acc.l + e;
-  acc.h = s + t;                          // renormalise
-  acc.l = t - (acc.h - s);
+  const float t = (acc.h - (s - v)) + (p - v);
+  acc.h = s;
+  acc.l += t + e;
 }
 
 #endif
