@@ -287,6 +287,9 @@ __global__ void __launch_bounds__(512) k_apply_df64(
 #pragma unroll
         for (int r = 0; r < G; ++r) {
           const float2 h = hv[r];
+          // about half of a group's slots are zero for a given row; every
+          // thread of the CTA sees the same value, so the skip is uniform
+          if (h.x == 0.f) continue;
           const float p = h.x * x.x;
           float e = fmaf(h.x, x.x, -p);
           e = fmaf(h.x, x.y, e);
