@@ -233,7 +233,7 @@ def run_ours(args, rank, world):
     n = s.N
     peak, peak_kind = peaks()
     roof = {}
-    for kind, vsz in (("umma_fp32", 4), ("tc_fp32", 4), ("tc_bf16", 2)):
+    for kind, vsz in (("umma_fp32", 4), ("tc_fp32", 4), ("umma_bf16", 2), ("tc_bf16", 2)):
         ms, cnt = op.kernel_time(kind)
         if cnt == 0:
             continue
@@ -287,6 +287,7 @@ def run_ours(args, rank, world):
            if (rank == 0 and world == 1 and not args.no_cpu) else None)
     if rank == 0:
         r32 = roof.get("umma_fp32") or roof["tc_fp32"]
+        kb = "umma_bf16" if "umma_bf16" in roof else ("tc_bf16" if "tc_bf16" in roof else None)
         kname = ("k_cheb_umma (one FP32 filter degree: tcgen05 SpMM, three-term BF16 "
                  "split, fused with the recurrence)" if "umma_fp32" in roof else
                  "k_cheb_tc<float, 5> (one FP32 filter degree: 3xTF32 mma.sync SpMM fused "
@@ -320,12 +321,13 @@ def run_ours(args, rank, world):
                          "bytes_per_launch": r32["bytes_per_launch"],
                          "flops_per_launch": r32["flops_per_launch"],
                          "launch_ms": r32["launch_ms"]},
-            "roofline_bf16_degree": ({"kernel": "k_cheb_tc<bf16, 5>",
-                                      "achieved": roof["tc_bf16"]["achieved"], "unit": "GB/s",
-                                      "frac": roof["tc_bf16"]["achieved"] / peak,
-                                      "launch_ms": roof["tc_bf16"]["launch_ms"],
-                                      "launches": roof["tc_bf16"]["launches"]}
-                                     if "tc_bf16" in roof else None),
+            "roofline_bf16_degree": ({"kernel": ("k_cheb_umma<1, bf16> (tcgen05)" if kb == "umma_bf16"
+                                                 else "k_cheb_tc<bf16, 5> (mma.sync)"),
+                                      "achieved": roof[kb]["achieved"], "unit": "GB/s",
+                                      "frac": roof[kb]["achieved"] / peak,
+                                      "launch_ms": roof[kb]["launch_ms"],
+                                      "launches": roof[kb]["launches"]}
+                                     if kb else None),
             "e2e": {"value": e2e, "unit": "s/SCF-iter", "h2d_bytes_per_step": int(nq * 8),
                     "d2h_bytes_per_step": int(2 * nq * 8 + p3 * k * 8),
                     "what": "same iterations with rho_in and rho_out passing through pinned "

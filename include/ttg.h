@@ -137,7 +137,8 @@ ttg_status ttg_op_elapsed_ms(ttg_op* op, int32_t slot0, int32_t slot1, float* ms
 #define TTG_KT_TC_FP32 1     /* mma.sync FP32 degree (3xTF32) */
 #define TTG_KT_TC_BF16 2     /* mma.sync BF16 degree */
 #define TTG_KT_ROWGROUP 3    /* CUDA-core row-group degree (any precision) */
-#define TTG_KT_KINDS 4
+#define TTG_KT_UMMA_BF16 4   /* tcgen05 BF16 degree */
+#define TTG_KT_KINDS 5
 ttg_status ttg_op_kernel_timing(ttg_op* op, int32_t enable);
 ttg_status ttg_op_kernel_time(ttg_op* op, int32_t kind, double* ms_total, int64_t* launches);
 

@@ -71,6 +71,33 @@ def test_umma_and_mma_sync_kernels_agree(small_system, monkeypatch):
     assert rel(out["umma"], out["mma_sync"]) < 5e-5
 
 
+def test_umma_bf16_degrees_agree_with_mma_sync(small_system, monkeypatch):
+    """BF16 degrees on tcgen05 (H rounded to BF16, one product per chunk)
+    against the mma.sync BF16 kernel and the FP64 oracle.  Both round H and
+    the block to BF16 and accumulate in FP32; they differ in summation order
+    only, so they agree far more closely than either agrees with FP64."""
+    s = small_system
+    k = 32
+    a, b, a0 = bounds(s)
+    X = np.random.default_rng(4).standard_normal((s.N, k))
+    out = {}
+    for name, disable in (("umma", "0"), ("mma_sync", "1")):
+        monkeypatch.setenv("TTG_DISABLE_UMMA", disable)
+        op = api.Operator(api.ProjectHamiltonianSparse.from_system(s), k)
+        try:
+            op.kernel_timing(True)
+            out[name] = run_filter(op, s, X, 6, a, b, a0, prec="bf16")
+            kind = "umma_bf16" if disable == "0" else "tc_bf16"
+            assert op.kernel_time(kind)[1] == 6        # every degree on the expected kernel
+        finally:
+            op.close()
+    ref = oracle.cheb_filter(s, X, 6, a, b, a0)
+    e_umma, e_tc = rel(out["umma"], ref), rel(out["umma"], out["mma_sync"])
+    print(f"bf16 degrees: tcgen05 vs FP64 {e_umma:.2e}, tcgen05 vs mma.sync {e_tc:.2e}")
+    assert e_umma < 5e-2
+    assert e_tc < 1e-2
+
+
 def test_umma_filter_after_potential_update():
     """New H values written by the device update (all formats, the tcgen05
     planes included) against the oracle's Hamiltonian for the same V_eff."""

@@ -698,7 +698,7 @@ ttg_status launch_cheb_step(ttg_op* op, int prec, const void* src, const void* x
                             int k, double alpha, double beta, double delta) {
   if (k <= 0 || k > op->max_k) return TTG_BAD_ARG;
   if (umma_supported(op, prec, k))
-    return launch_cheb_umma(op, src, xold, dst, k, alpha, beta, delta);
+    return launch_cheb_umma(op, prec, src, xold, dst, k, alpha, beta, delta);
   if (tc_supported(op, prec, k))
     return launch_cheb_tc(op, prec, src, xold, dst, k, alpha, beta, delta);
   if (prec == TTG_PREC_FP64) {

@@ -44,6 +44,7 @@
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -151,12 +152,17 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// NT = 3: FP32 degree (three BF16 terms of H and of the block, six
+// products); NT = 1: BF16 degree (H rounded to BF16, the BF16 block itself,
+// one product).  TIO is the block's element type (float / bf16).
+template <int NT, typename TIO>
 __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     const int64_t* __restrict__ tptr, const int* __restrict__ tcol, const int* __restrict__ rowmap,
     const int* __restrict__ order, const __nv_bfloat16* __restrict__ hpl,
-    const __nv_bfloat16* __restrict__ xpl, int64_t pstride, int ps, const float* __restrict__ src,
-    const float* xold, float* dst, int k, int64_t ld, float alpha, float beta, float delta,
+    const __nv_bfloat16* __restrict__ xpl, int64_t pstride, int ps, const TIO* __restrict__ src,
+    const TIO* xold, TIO* dst, int k, int64_t ld, float alpha, float beta, float delta,
     uint32_t tmem_cols, int nh, int nb, int* __restrict__ err) {
+  constexpr int HB = NT * 2 * PLANE_ELEMS;    // H bytes per chunk: the first NT planes
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // rings start on a 1024-byte boundary (swizzle atoms; descriptor base offset 0):
   // nb gathered-row stages, then nh H stages
@@ -174,7 +180,7 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
   const int tile = __ldg(order + blockIdx.x), tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int natoms = (k + kAtom - 1) / kAtom;
   const int bplane = natoms * kAtomBytes;               // one gathered plane
-  const int bstage = 3 * bplane;
+  const int bstage = NT * bplane;
   unsigned char* hring = smem + nb * bstage;
   const int64_t c_first = tptr[tile] / UK;
   const int nch = (int)((tptr[tile + 1] - tptr[tile]) / UK);
@@ -218,12 +224,12 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
         }
         const uint32_t fb = smem_u32(&full[c % nd]);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb),
-                     "r"(CHUNK_BYTES) : "memory");
+                     "r"(HB) : "memory");
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
             " [%0], [%1], %2, [%3], %4;"
-            ::"r"(smem_u32(hring + s * CHUNK_BYTES)), "l"(hpl + (c_first + c) * CHUNK_ELEMS),
-              "r"(CHUNK_BYTES), "r"(fb), "l"(pol_stream)
+            ::"r"(smem_u32(hring + s * HB)), "l"(hpl + (c_first + c) * CHUNK_ELEMS),
+              "r"(HB), "r"(fb), "l"(pol_stream)
             : "memory");
       }
     }
@@ -276,7 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
             for (int a = 0; a < natoms; ++a) {
               if (a * 8 + lj < ngrp) {
 #pragma unroll
-                for (int pl = 0; pl < 3; ++pl)
+                for (int pl = 0; pl < NT; ++pl)
                   asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;"
                                ::"r"(drow + (uint32_t)(pl * bplane + a * kAtomBytes)),
                                  "l"(xs + pl * pstride + a * kAtom), "l"(pol_keep)
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     const uint32_t idesc = instr_desc(UR, k);
     const uint64_t da_hi = smem_desc(0), db_hi = smem_desc_sw128(0);
     const uint32_t a_first = smem_u32(hring) >> 4, b_first = smem_u32(smem) >> 4;
-    const uint32_t a_end = a_first + nh * (CHUNK_BYTES >> 4);
+    const uint32_t a_end = a_first + nh * (HB >> 4);
     const uint32_t b_end = b_first + nb * (bstage >> 4);
     const uint32_t bpl = (uint32_t)bplane >> 4, apl = (2 * PLANE_ELEMS) >> 4;
     const uint32_t done0 = smem_u32(&done[0]);
@@ -334,9 +340,10 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
                               da_hi | a_lo, da_hi | (a_lo + apl), da_hi | a_lo};
       const uint64_t db[6] = {db_hi | (b_lo + bpl), db_hi | (b_lo + 2 * bpl), db_hi | b_lo,
                               db_hi | (b_lo + bpl), db_hi | b_lo, db_hi | b_lo};
+      constexpr int q0 = NT == 3 ? 0 : 5;       // NT = 1: (0,0) only
 #pragma unroll
-      for (int q = 0; q < 6; ++q) {
-        const uint32_t acc = (c > 0 || q > 0) ? 1u : 0u;
+      for (int q = q0; q < 6; ++q) {
+        const uint32_t acc = (c > 0 || q > q0) ? 1u : 0u;
         asm volatile(
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
@@ -346,7 +353,7 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
           ::"r"(done0 + 8 * sd)
           : "memory");
-      a_lo += CHUNK_BYTES >> 4;
+      a_lo += HB >> 4;
       if (a_lo == a_end) a_lo = a_first;
       b_lo += bstage >> 4;
       if (b_lo == b_end) b_lo = b_first;
@@ -386,22 +393,45 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     }
     if (row >= 0) {
       const int64_t off = (int64_t)row * ld + c0;
+      if constexpr (std::is_same<TIO, float>::value) {
 #pragma unroll
-      for (int j = 0; j < 16; j += 4) {
-        const float4 y = *reinterpret_cast<const float4*>(src + off + j);
-        float4 o;
-        o.x = alpha * __uint_as_float(v[j]) + beta * y.x;
-        o.y = alpha * __uint_as_float(v[j + 1]) + beta * y.y;
-        o.z = alpha * __uint_as_float(v[j + 2]) + beta * y.z;
-        o.w = alpha * __uint_as_float(v[j + 3]) + beta * y.w;
-        if (delta != 0.f) {
-          const float4 x = *reinterpret_cast<const float4*>(xold + off + j);
-          o.x = fmaf(delta, x.x, o.x);
-          o.y = fmaf(delta, x.y, o.y);
-          o.z = fmaf(delta, x.z, o.z);
-          o.w = fmaf(delta, x.w, o.w);
+        for (int j = 0; j < 16; j += 4) {
+          const float4 y = *reinterpret_cast<const float4*>(src + off + j);
+          float4 o;
+          o.x = alpha * __uint_as_float(v[j]) + beta * y.x;
+          o.y = alpha * __uint_as_float(v[j + 1]) + beta * y.y;
+          o.z = alpha * __uint_as_float(v[j + 2]) + beta * y.z;
+          o.w = alpha * __uint_as_float(v[j + 3]) + beta * y.w;
+          if (delta != 0.f) {
+            const float4 x = *reinterpret_cast<const float4*>(xold + off + j);
+            o.x = fmaf(delta, x.x, o.x);
+            o.y = fmaf(delta, x.y, o.y);
+            o.z = fmaf(delta, x.z, o.z);
+            o.w = fmaf(delta, x.w, o.w);
+          }
+          *reinterpret_cast<float4*>(dst + off + j) = o;
         }
-        *reinterpret_cast<float4*>(dst + off + j) = o;
+      } else {
+        // BF16 block: 8 values (16 bytes) per access, arithmetic in FP32
+#pragma unroll
+        for (int j = 0; j < 16; j += 8) {
+          const uint4 yu = *reinterpret_cast<const uint4*>(src + off + j);
+          uint4 xu = make_uint4(0u, 0u, 0u, 0u);
+          if (delta != 0.f) xu = *reinterpret_cast<const uint4*>(xold + off + j);
+          const __nv_bfloat162* y2 = reinterpret_cast<const __nv_bfloat162*>(&yu);
+          const __nv_bfloat162* x2 = reinterpret_cast<const __nv_bfloat162*>(&xu);
+          uint4 ou;
+          __nv_bfloat162* o2 = reinterpret_cast<__nv_bfloat162*>(&ou);
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const float2 yf = __bfloat1622float2(y2[t]);
+            const float2 xf = __bfloat1622float2(x2[t]);
+            const float a0 = fmaf(delta, xf.x, alpha * __uint_as_float(v[j + 2 * t]) + beta * yf.x);
+            const float a1 = fmaf(delta, xf.y, alpha * __uint_as_float(v[j + 2 * t + 1]) + beta * yf.y);
+            o2[t] = __floats2bfloat162_rn(a0, a1);
+          }
+          *reinterpret_cast<uint4*>(dst + off + j) = ou;
+        }
       }
     }
   }
@@ -602,53 +632,69 @@ ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int3
 }
 
 bool umma_supported(const ttg_op* op, int prec, int k) {
-  return prec == TTG_PREC_FP32 && op->umma.n_tiles > 0 && !op->tc_disabled && k >= 16 &&
+  return (prec == TTG_PREC_FP32 || prec == TTG_PREC_BF16) && op->umma.n_tiles > 0 && !op->tc_disabled && k >= 16 &&
          k <= 256 && k % 16 == 0 && k <= op->ld;
 }
 
-ttg_status launch_cheb_umma(ttg_op* op, const void* src, const void* xold, void* dst, int k,
-                            double alpha, double beta, double delta) {
+namespace {
+
+template <int NT, typename TIO>
+ttg_status launch_umma_t(ttg_op* op, const __nv_bfloat16* xpl, int64_t pstride, int ps,
+                         const void* src, const void* xold, void* dst, int k, double alpha,
+                         double beta, double delta) {
   UmmaOp& U = op->umma;
-  const int ps = k;                                  // multiple of 16
+  constexpr int HB = NT * 2 * PLANE_ELEMS;
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(k_cheb_umma<NT, TIO>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBudget);
+  });
+  if (attr_err != cudaSuccess) return TTG_CUDA_ERR;
+  uint32_t cols = 32;
+  while ((int)cols < k) cols <<= 1;
+  const int natoms = (k + kAtom - 1) / kAtom;
+  const int bstage = NT * natoms * kAtomBytes;
+  // eight H stages (the H copies run ahead of the rows), the rest to the
+  // row stages, then what is left to more H stages (1024 bytes go to alignment)
+  const int avail = kSmemBudget - 1024;
+  const int nb = std::min(kMaxB, (avail - 8 * HB) / bstage);
+  const int nh = std::min(kMaxH, (avail - nb * bstage) / HB);
+  if (nb < 3 || nh < 3) return TTG_BAD_ARG;
+  const size_t smem = (size_t)nb * bstage + (size_t)nh * HB + 1024;
+  TTG_TRY(kt_begin(op, NT == 3 ? TTG_KT_UMMA_FP32 : TTG_KT_UMMA_BF16));
+  k_cheb_umma<NT, TIO><<<(unsigned)U.n_tiles, kThreads, smem, op->stream>>>(
+      U.tptr.as<int64_t>(), U.tcol.as<int>(), U.rowmap.as<int>(), U.order.as<int>(),
+      U.hpl.as<__nv_bfloat16>(), xpl, pstride, ps, reinterpret_cast<const TIO*>(src),
+      reinterpret_cast<const TIO*>(xold), reinterpret_cast<TIO*>(dst), k, op->ld, (float)alpha,
+      (float)beta, (float)delta, cols, nh, nb, U.err.as<int>()); TTG_COUNT();
+  TTG_LAUNCHED(op);
+  TTG_TRY(kt_end(op));
+  return TTG_OK;
+}
+
+}  // namespace
+
+ttg_status launch_cheb_umma(ttg_op* op, int prec, const void* src, const void* xold, void* dst,
+                            int k, double alpha, double beta, double delta) {
+  UmmaOp& U = op->umma;
   const int64_t rows = op->n + op->nproj;
+  if (prec == TTG_PREC_BF16)   // the block's rows are gathered as they are (row stride ld)
+    return launch_umma_t<1, __nv_bfloat16>(op, reinterpret_cast<const __nv_bfloat16*>(src), 0,
+                                           (int)op->ld, src, xold, dst, k, alpha, beta, delta);
+  const int ps = k;                                  // multiple of 16
   const int64_t pstride = rows * ps;
   const size_t need = (size_t)3 * pstride * sizeof(uint16_t);
   if (U.xpl.bytes < need) {
     TTG_TRY(U.xpl.alloc(need));
     op->device_bytes += (int64_t)need;
   }
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
-  std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(k_cheb_umma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kSmemBudget);
-  });
-  if (attr_err != cudaSuccess) return TTG_CUDA_ERR;
   const int grid_s = (int)std::min<int64_t>((rows * ps + 255) / 256, 152 * 16);
   k_split3<<<grid_s, 256, 0, op->stream>>>(reinterpret_cast<const float*>(src), rows, k, op->ld,
                                            U.xpl.as<__nv_bfloat16>(), ps, pstride); TTG_COUNT();
   TTG_LAUNCHED(op);
-  uint32_t cols = 32;
-  while ((int)cols < k) cols <<= 1;
-  const int natoms = (k + kAtom - 1) / kAtom;
-  const int bstage = 3 * natoms * kAtomBytes;
-  // eight H stages (the H copies run ahead of the rows), the rest to the
-  // row stages, then what is left to more H stages (1024 bytes go to alignment)
-  const int avail = kSmemBudget - 1024;
-  const int nb = std::min(kMaxB, (avail - 8 * CHUNK_BYTES) / bstage);
-  const int nh = std::min(kMaxH, (avail - nb * bstage) / CHUNK_BYTES);
-  if (nb < 3 || nh < 3) return TTG_BAD_ARG;
-  const size_t smem = (size_t)nb * bstage + (size_t)nh * CHUNK_BYTES + 1024;
-  TTG_TRY(kt_begin(op, TTG_KT_UMMA_FP32));
-  k_cheb_umma<<<(unsigned)U.n_tiles, kThreads, smem, op->stream>>>(
-      U.tptr.as<int64_t>(), U.tcol.as<int>(), U.rowmap.as<int>(), U.order.as<int>(),
-      U.hpl.as<__nv_bfloat16>(), U.xpl.as<__nv_bfloat16>(), pstride, ps,
-      reinterpret_cast<const float*>(src), reinterpret_cast<const float*>(xold),
-      reinterpret_cast<float*>(dst), k, op->ld, (float)alpha, (float)beta, (float)delta, cols, nh,
-      nb, U.err.as<int>()); TTG_COUNT();
-  TTG_LAUNCHED(op);
-  TTG_TRY(kt_end(op));
-  return TTG_OK;
+  return launch_umma_t<3, float>(op, U.xpl.as<__nv_bfloat16>(), pstride, ps, src, xold, dst, k,
+                                 alpha, beta, delta);
 }
 
 ttg_status umma_check_error(ttg_op* op) {

@@ -233,8 +233,8 @@ ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int3
                             const double* hv, int32_t nproj, const int64_t* cp, const int32_t* cc,
                             const double* cv, const int32_t* dims);
 bool umma_supported(const ttg_op* op, int prec, int k);
-ttg_status launch_cheb_umma(ttg_op* op, const void* src, const void* xold, void* dst, int k,
-                            double alpha, double beta, double delta);
+ttg_status launch_cheb_umma(ttg_op* op, int prec, const void* src, const void* xold, void* dst,
+                            int k, double alpha, double beta, double delta);
 ttg_status umma_check_error(ttg_op* op);
 ttg_status launch_cheb_tc(ttg_op* op, int prec, const void* src, const void* xold, void* dst,
                           int k, double alpha, double beta, double delta);
