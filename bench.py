@@ -50,7 +50,7 @@ MIX_DEPTH = 10           # Anderson history (the reference example's history=10)
 # the 64-atom operator with its 160-column block (profile_workload --workload
 # atoms64 --prec fp32 --degrees 1): bytes / 3,760,928 slots; scaled to the
 # timed operator's slots
-TRAFFIC_PER_SLOT_UMMA = (3.63e9 + 40.42e6) / 3760928
+TRAFFIC_PER_SLOT_UMMA = (3.11e9 + 31.32e6) / 3760928
 MAX_ITER = 60
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
