@@ -668,9 +668,23 @@ ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_statu
 }
 
 ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* d_status) {
-  // Householder + QL in FP32 (fast pipes), then two Ogita-Aishima refinement
-  // steps in FP64 (k x k GEMMs over all SMs) restore FP64 accuracy.
   const int64_t kk = (int64_t)k * k;
+  if (k <= 2048 && (int64_t)op->kk2.bytes >= kk * 8 &&
+      (int64_t)op->scal.bytes >= (kScalJacobi + k) * (int64_t)sizeof(double)) {
+    // the STHOSVD eigensolver with all k pairs (eig.cu): FP64 Householder on
+    // a cluster of 8 CTAs, multisection, inverse iteration, Cholesky QR2.
+    // FP64-accurate without refinement, and at k = 160 a little faster than
+    // the FP32 QL + refinement below (about 1 ms per Rayleigh-Ritz pass).
+    // A is overwritten.
+    double* wtmp = op->scal.as<double>() + kScalJacobi;
+    double* Vd = op->kk2.as<double>();
+    TTG_TRY(sym_topk(op, A, k, k, wtmp, Vd, d_status));
+    k_sort_eig<<<(k + 127) / 128, 128, 0, op->stream>>>(wtmp, Vd, w, V, k); TTG_COUNT();
+    TTG_LAUNCHED(op);
+    return TTG_OK;
+  }
+  // k > 2048: Householder + QL in FP32 (fast pipes), then two Ogita-Aishima
+  // refinement steps (k x k GEMMs over all SMs) restore FP64 accuracy.
   const size_t need_f = (size_t)(2 * kk + 8 * (int64_t)k + 64) * sizeof(float);
   if ((int64_t)op->scal.bytes < (kScalJacobi + k) * (int64_t)sizeof(double) ||
       (int64_t)op->kk2.bytes < kk * 8 || op->kk3.bytes < need_f)
