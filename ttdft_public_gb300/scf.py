@@ -311,6 +311,7 @@ class Scf:
         v0 = np.random.default_rng(cfg.seed + 1).uniform(0, 1, self.s.N)
         occ_idx = min(int(self.ne / 2.0 + 10), k - 1)               # main.cc:686-688
         hist_in, hist_out = [], []
+        self._mix_res, self._mix_gram = {}, {}
         upper = 1e16
         err_upper = 1e16
         lower_wanted = lower_unwanted = None
@@ -430,16 +431,38 @@ class Scf:
         (dft/AndersonMixing.cc:150-316): weighted least squares on the
         residuals F = rho_out - rho_in, then |alpha rho_out_bar + (1-alpha) rho_in_bar|."""
         h = len(hin)
-        F = [self.lincomb([hout[i], hin[i]], [1.0, -1.0], self._zeros()) for i in range(h)]
+        # Residuals F_i and their weighted Gram matrix are kept across
+        # iterations (an entry stays while its densities are in the history),
+        # so each call forms one new residual and h new inner products instead
+        # of h residuals, h - 1 differences and h^2 inner products.  With
+        # D_m = F_n - F_{n-1-m}: <D_m, D_k> = G_nn - G_nk' - G_m'n + G_m'k'.
+        keys = [(id(hin[i]), id(hout[i])) for i in range(h)]
+        res = self._mix_res
+        for key in [key for key in res if key not in keys]:
+            del res[key]
+        self._mix_gram = {kk: v for kk, v in self._mix_gram.items()
+                          if kk[0] in res and kk[1] in res}
+        for i, key in enumerate(keys):
+            if key not in res:   # the entry holds its densities, so ids stay unique
+                res[key] = (hin[i], hout[i],
+                            self.lincomb([hout[i], hin[i]], [1.0, -1.0], self._zeros()))
+        G = np.zeros((h, h))
+        for i in range(h):
+            for j in range(i, h):
+                kk = (keys[i], keys[j])
+                if kk not in self._mix_gram:
+                    self._mix_gram[kk] = self.integrate(res[keys[i]][2], res[keys[j]][2])
+                G[i, j] = G[j, i] = self._mix_gram[kk]
         n = h - 1
         A = np.zeros((n, n))
         b = np.zeros(n)
-        Fn = F[h - 1]
-        D = [self.lincomb([Fn, F[h - 2 - mm]], [1.0, -1.0], self._zeros()) for mm in range(n)]
+        last = h - 1
         for mm in range(n):
+            pm = h - 2 - mm
+            b[mm] = G[last, last] - G[pm, last]
             for kk in range(n):
-                A[mm, kk] = self.integrate(D[mm], D[kk])
-            b[mm] = self.integrate(D[mm], Fn)
+                pk = h - 2 - kk
+                A[mm, kk] = G[last, last] - G[last, pk] - G[pm, last] + G[pm, pk]
         c = solve_small(A, b) if n > 0 else np.zeros(0)
         self.mix_coef = c
         # rho_in_bar = rho_in_n + sum c_k (rho_in_k - rho_in_n), same for out
