@@ -59,7 +59,7 @@ def test_training_fits_a_smooth_function():
 
 @pytest.mark.skipif(learned.load_default() is None, reason="no trained model packaged")
 def test_learned_guess_gains_over_superposition():
-    """A held-out 16-atom configuration, judged by the FP64 SCF: the learned
+    """A held-out 16-atom configuration, checked against the FP64 SCF: the learned
     start is closer to the converged density, needs no more SCF iterations,
     and both starts reach the same energy (both converged to 1e-7 Ha/atom
     between iterations, so that the slow Anderson tail leaves them well inside
