@@ -1,14 +1,14 @@
-// FP32-accurate filter degree on the fifth-generation tensor cores
-// (tcgen05.mma, accumulator in tensor memory), for the FP32 degrees of the
-// Chebyshev filter (ChebyShevFilter.cc:97-170: Ynew = alpha (H Y) + beta Y +
-// delta X).
+// Chebyshev filter degrees on the fifth-generation tensor cores
+// (tcgen05.mma, accumulator in tensor memory): Ynew = alpha (H Y) + beta Y +
+// delta X (ChebyShevFilter.cc:97-170).  FP32 degrees run FP32-accurate on
+// BF16 MMAs (three-term split below); BF16 degrees run one BF16 product.
 //
 // Tiles.  128 rows per tile (a 4 x 4 x 8 block of the Tucker index, or 128
 // consecutive rows without Tucker ranks); the tile's sorted column union is
 // padded to chunks of 16 slots.  A chunk is one MMA step: M = 128 rows,
 // N = k states, K = 16 slots.
 //
-// Precision.  Every FP32 value v is split into three BF16 terms
+// Precision (FP32 degrees).  Every FP32 value v is split into three BF16 terms
 // v = v0 + v1 + v2 (|v1| <= 2^-9 |v|, |v2| <= 2^-18 |v|).  The product H Y
 // is accumulated in FP32 from the six term products of order <= 2
 // (v0w0, v0w1, v1w0, v1w1, v0w2, v2w0); the dropped ones are below 2^-26 of
@@ -30,14 +30,18 @@
 //    own copies and fences them for the async proxy before it arrives;
 //  - warp 2, one thread: waits for each chunk's "full" mbarrier in order and
 //    publishes the count of ready chunks in shared memory;
-//  - warp 1, one thread: six MMAs and one commit (to the chunk's "done"
+//  - warp 1, one thread: six MMAs (one for BF16) and one commit (to the chunk's "done"
 //    mbarrier) per chunk.  It never waits on an mbarrier itself: such a wait
 //    queues behind its outstanding MMAs (about 0.1 us per chunk).
 // Waits off the critical path back off with nanosleep: tight polling by many
 // threads slows every mbarrier operation of the CTA.  After the last chunk,
 // warps 0-3 (one per 32 TMEM lanes) read the accumulator from tensor memory
 // and apply the recurrence in FP32.
-// Every mbarrier wait is bounded; a wait that runs out sets an error word.
+// BF16 degrees (NT = 1) use H's plane 0 (its BF16 rounding), gather the
+// BF16 block's rows as they are, issue one MMA per chunk and round the
+// epilogue's FP32 result to BF16.
+// Every wait (mbarrier or the ready count) is bounded; a wait that runs out
+// sets an error word.
 
 #include <cuda_bf16.h>
 

@@ -110,9 +110,10 @@ struct TileOp {
   DevBuf v16;      // bf16,  [chunk][8 n-tiles][32 lanes][4]
 };
 
-// 128-row tiles for the tcgen05 FP32 filter degree (spmm_umma.cu): H as three
-// BF16 planes per 16-slot chunk in the MMA operand layout, and the block's
-// three BF16 planes that the kernel gathers.
+// 128-row tiles for the tcgen05 filter degrees (spmm_umma.cu): H as three
+// BF16 planes per 16-slot chunk in the MMA operand layout (FP32 degrees use
+// all three, BF16 degrees plane 0), and the block's three BF16 planes that
+// the FP32 degrees gather.
 struct UmmaOp {
   int64_t n_tiles = 0;
   int64_t slots = 0;
@@ -175,7 +176,7 @@ struct ttg_op {
   int64_t nnz_h = 0, nnz_c = 0;
   ttg::RowGroups rg;
   ttg::TileOp tiles;          // tensor-core format (FP32/BF16 degrees)
-  ttg::UmmaOp umma;           // tcgen05 format (FP32 degrees)
+  ttg::UmmaOp umma;           // tcgen05 format (FP32 and BF16 degrees)
   bool tc_disabled = false;   // TTG_DISABLE_TC=1: CUDA-core kernels only
   bool keep_pattern = false;  // Tucker ranks given: keep the pattern for value updates
   ttg::Pattern pattern;
