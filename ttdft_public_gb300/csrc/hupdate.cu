@@ -83,9 +83,18 @@ __global__ void k_update_values(UpdateArgs a) {
     if (xp >= 0 && yp >= 0 && zp >= 0) {
       const double* t2 = a.T2 + ((int64_t)yp * a.nxp + xp) * a.rc;
       const double* pz = a.PZp + (int64_t)zp * a.rc;
-      double s = 0.0;
-      for (int c = 0; c < a.rc; ++c) s = fma(pz[c], t2[c], s);
-      val += s;
+      // four independent partial sums: the FP64 FMA chain of one sum would
+      // otherwise serialise the rc terms of every entry
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      int c = 0;
+      for (; c + 3 < a.rc; c += 4) {
+        s0 = fma(pz[c], t2[c], s0);
+        s1 = fma(pz[c + 1], t2[c + 1], s1);
+        s2 = fma(pz[c + 2], t2[c + 2], s2);
+        s3 = fma(pz[c + 3], t2[c + 3], s3);
+      }
+      for (; c < a.rc; ++c) s0 = fma(pz[c], t2[c], s0);
+      val += (s0 + s1) + (s2 + s3);
     }
     const int p = a.rg_pos[e];
     a.v64[p] = val;
