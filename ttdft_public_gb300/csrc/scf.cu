@@ -420,21 +420,6 @@ __global__ void __launch_bounds__(256) k_hartree_energy_slab(
   }
 }
 
-__global__ void k_dot(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
-                      double* out) {
-  __shared__ double red[32];
-  double s = 0.0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += a[i] * b[i];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-    *out = t;
-  }
-}
-
 __global__ void k_diag_sum(const double* __restrict__ A, int n, double* out) {
   if (threadIdx.x == 0) {
     double s = 0.0;

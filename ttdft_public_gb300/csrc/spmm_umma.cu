@@ -63,7 +63,6 @@ constexpr int UR = 128;                       // rows per tile (MMA M)
 constexpr int UK = 16;                        // slots per chunk (MMA K)
 constexpr int PLANE_ELEMS = UR * UK;          // 2048 BF16 = 4096 bytes
 constexpr int CHUNK_ELEMS = 3 * PLANE_ELEMS;  // three planes
-constexpr int CHUNK_BYTES = 2 * CHUNK_ELEMS;  // 12288
 constexpr int kMaxH = 12;                     // H ring stages (12 KB each)
 constexpr int kMaxB = 8;                      // gathered-row ring stages
 constexpr int kSmemBudget = 227 * 1024 - 1024;
@@ -318,7 +317,7 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
                      : "memory");
       }
     }
-  } else if (lane == 0) {
+  } else if (warp == kMmaWarp && lane == 0) {
     // MMA thread: six MMAs per chunk (term pairs, smallest products first),
     // committed to the chunk's "done" barrier.  Its per-chunk work is kept to
     // a short dependency chain (stage addresses and descriptors advance by
