@@ -89,3 +89,23 @@ def test_oracle_hamiltonian_values(tiny_system):
     ref = c.kin + np.einsum("abc,ae,be,ce->e", core, P[0][:, xi, xj], P[1][:, yi, yj],
                             P[2][:, zi, zj], optimize=True)
     assert np.abs(H.val - ref).max() < 1e-12 * np.abs(ref).max()
+
+
+def test_anderson_system_from_gram_matches_direct_differences():
+    """The mixing system built from the residuals' Gram matrix (as the GPU
+    driver keeps it across iterations) equals the one built from the
+    differences D_m = F_n - F_m directly (as the oracle does)."""
+    from ttdft_public_gb300.scf import anderson_system
+    rng = np.random.default_rng(11)
+    h, npts = 7, 500
+    w = rng.uniform(0.5, 2.0, npts)
+    F = [rng.standard_normal(npts) * (1.0 + 0.1 * i) for i in range(h)]
+    dot = lambda a, b: float(np.sum(a * b * w))
+    G = np.array([[dot(F[i], F[j]) for j in range(h)] for i in range(h)])
+    A, b = anderson_system(G)
+    D = [F[h - 1] - F[h - 2 - m] for m in range(h - 1)]
+    A_ref = np.array([[dot(D[i], D[j]) for j in range(h - 1)] for i in range(h - 1)])
+    b_ref = np.array([dot(D[i], F[h - 1]) for i in range(h - 1)])
+    scale = np.abs(G).max()
+    assert np.abs(A - A_ref).max() < 1e-12 * scale
+    assert np.abs(b - b_ref).max() < 1e-12 * scale

@@ -454,15 +454,7 @@ class Scf:
                     self._mix_gram[kk] = self.integrate(res[keys[i]][2], res[keys[j]][2])
                 G[i, j] = G[j, i] = self._mix_gram[kk]
         n = h - 1
-        A = np.zeros((n, n))
-        b = np.zeros(n)
-        last = h - 1
-        for mm in range(n):
-            pm = h - 2 - mm
-            b[mm] = G[last, last] - G[pm, last]
-            for kk in range(n):
-                pk = h - 2 - kk
-                A[mm, kk] = G[last, last] - G[last, pk] - G[pm, last] + G[pm, pk]
+        A, b = anderson_system(G)
         c = solve_small(A, b) if n > 0 else np.zeros(0)
         self.mix_coef = c
         # rho_in_bar = rho_in_n + sum c_k (rho_in_k - rho_in_n), same for out
@@ -473,6 +465,25 @@ class Scf:
         fields = fin + fout
         coef = [(1.0 - a) * x for x in cin] + [a * x for x in cin]
         return self.lincomb(fields, coef, self._zeros(), take_abs=True)
+
+
+def anderson_system(G):
+    """The mixing least-squares system of AndersonMixing::computeMixingConstants
+    (dft/AndersonMixing.cc:150-265) from the weighted Gram matrix G of the
+    residuals F_0 .. F_{h-1} (oldest first): with D_m = F_{h-1} - F_{h-2-m},
+    A[m, k] = <D_m, D_k> and b[m] = <D_m, F_{h-1}>, expanded in G."""
+    h = G.shape[0]
+    n = h - 1
+    A = np.zeros((n, n))
+    b = np.zeros(n)
+    last = h - 1
+    for mm in range(n):
+        pm = h - 2 - mm
+        b[mm] = G[last, last] - G[pm, last]
+        for kk in range(n):
+            pk = h - 2 - kk
+            A[mm, kk] = G[last, last] - G[last, pk] - G[pm, last] + G[pm, pk]
+    return A, b
 
 
 def solve_small(A, b):
