@@ -161,3 +161,36 @@ def test_sthosvd_degenerate_spectrum_fixed_rank(gpu_scf):
     # the 1e-6 component's Gram eigenvalue is 1e-12 of the largest, so its
     # eigenvector carries ~1e-4 error from FP64 rounding of the Gram matrix
     assert np.abs(rec - T).max() < 1e-9 * np.abs(T).max()
+
+
+def test_tucker_files_restart_the_scf(tmp_path):
+    """write_out_rho -> initialize_rho_tucker (main.cc:1528-1632,
+    dft/InitialGuess.cc:764-904): the converged output density written as
+    Tucker files in the reference's format and read back as the initial
+    guess starts the next run next to the fixed point, and it converges to
+    the same energy in fewer iterations."""
+    import shutil
+    from ttdft_public_gb300 import tucker_io
+    spec = system.small_spec(name="scf", n_atoms=2, box=10.0, n_el=16, rank=8, n_states=16,
+                             degree=12, seed=3)
+    s = system.build_system(spec)
+    g = scf.Scf(s, scf.ScfConfig(max_iter=12))
+    try:
+        res = g.run()
+        names = g.write_density(str(tmp_path))
+        e_sad = g.start_error()
+    finally:
+        g.close()
+    assert [n.split("/")[-1] for n in names] == ["rank_8_core", "rank_8_factor_x",
+                                                "rank_8_factor_y", "rank_8_factor_z"]
+    for src, dst in zip(names, [tucker_io.CORE_IN, *tucker_io.FACTOR_IN]):
+        shutil.copy(src, str(tmp_path / dst))
+    g2 = scf.Scf(s, scf.ScfConfig(max_iter=12, guess="tucker", tucker_dir=str(tmp_path)))
+    try:
+        res2 = g2.run()
+        assert g2.guess_used == "tucker"
+        assert g2.start_error() < 0.1 * e_sad
+        assert res2["iterations"] < res["iterations"]
+        assert abs(res2["energy"] - res["energy"]) / spec.n_atoms < 1e-5
+    finally:
+        g2.close()

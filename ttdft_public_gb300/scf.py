@@ -32,7 +32,7 @@ import time
 
 import numpy as np
 
-from . import _lib, api
+from . import _lib, api, tucker_io
 from ._lib import check
 from .kernel_expansion import coulomb_expansion
 
@@ -68,8 +68,11 @@ class ScfConfig:
     ion_width: float = 1.0            # Gaussian ionic charges (bohr)
     sad_width: float = 1.0            # width of the atomic densities (bohr)
     filter: str = "fp64"              # fp64 | fp32 | mixed (BF16 first quarter)
-    guess: str = "sad"                # sad | learned (falls back to sad without a model)
+    guess: str = "sad"                # sad | learned (falls back to sad without a model) | tucker
     model_path: str = ""              # learned-guess model ("" = the packaged one)
+    # guess "tucker": directory holding tucker_input_core and
+    # tucker_input_factor_{x,y,z} (InitialGuess::initialize_rho_tucker)
+    tucker_dir: str = ""
     seed: int = 0
 
 
@@ -241,6 +244,16 @@ class Scf:
     # ---- SCF pieces -----------------------------------------------------------
     def initial_density(self):
         spec, cfg = self.s.spec, self.cfg
+        if cfg.guess == "tucker":
+            # InitialGuess::initialize_rho_tucker (dft/InitialGuess.cc:764-904):
+            # the factor columns' splines at the quadrature points, then the
+            # Tucker reconstruction on the device
+            core, fac = tucker_io.read_density(cfg.tucker_dir)
+            Uq = [tucker_io.factors_at(x, u, self.xq[d]) for d, (x, u) in enumerate(fac)]
+            rho = self.reconstruct(core.reshape(-1, order="F"), Uq, list(core.shape), self.qdims)
+            self.guess_used = "tucker"
+            rho *= self.ne / self.integrate(rho)                   # main.cc:674-680
+            return rho
         w = cfg.sad_width
         norm = spec.z_val / (math.pi * w * w) ** 1.5
         f = [np.stack([np.exp(-(self.xq[d] - a[d]) ** 2 / (w * w)) for a in self.s.atoms])
@@ -284,6 +297,7 @@ class Scf:
         at the quad points for the Hartree term."""
         rho_n = api.density(self.op, X, occ, self.s.basis).reshape(-1)
         rho_nd = self._dev(rho_n)
+        self.rho_nodal = rho_nd
         G, U, r = self.sthosvd(rho_nd, self.ndims, self.cfg.rho_out_eps, self.cfg.rho_out_rank_cap)
         Uq = [self.s.basis[d].fem.interp_matrix() @ U[d] for d in range(3)]
         raw = self.reconstruct(G, Uq, r, self.qdims)
@@ -425,6 +439,20 @@ class Scf:
                 and history[-1]["de_atom"] < self.cfg.tol_e_atom
                 and history[-1]["drho2"] < self.cfg.tol_drho2,
                 "wall_s": time.perf_counter() - t_start}
+
+    def write_density(self, dirpath):
+        """write_out_rho (main.cc:1528-1632): the last output density on the
+        nodes as a Tucker tensor at the reference's output ranks, in its file
+        format (rank_<r>_core, rank_<r>_factor_{x,y,z}).  One rank cap serves
+        all three directions (the largest of the per-direction ranks; they
+        are equal on cubic grids)."""
+        if getattr(self, "rho_nodal", None) is None:
+            raise RuntimeError("no output density yet: run an SCF iteration first")
+        cap = max(tucker_io.output_ranks([int(n) for n in self.ndims]))
+        G, U, r = self.sthosvd(self.rho_nodal, self.ndims, 0.0, cap)
+        return tucker_io.write_density(dirpath, G.reshape(r, order="F"),
+                                       [self.s.basis[d].fem.nodes for d in range(3)], U,
+                                       [self.s.basis[d].r for d in range(3)])
 
     def anderson(self, hin, hout):
         """AndersonMixing::computeMixingConstants + computeRhoIn
