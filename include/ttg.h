@@ -43,7 +43,7 @@ typedef enum {
   TTG_PREC_FP64 = 0,   /* H and the block in FP64, FP64 accumulation */
   TTG_PREC_FP32 = 1,   /* H and the block in FP32, FP32 accumulation */
   TTG_PREC_BF16 = 2,   /* H and the block stored in BF16, FP32 accumulation */
-  TTG_PREC_DF64 = 3    /* FP64 values as pairs of FP32 (~44 bits) on the FP32 pipes */
+  TTG_PREC_DF64 = 3    /* FP64 values as pairs of FP32 (~47 bits) on the FP32 pipes */
 } ttg_prec;
 
 /* Precision schedule of one Chebyshev filter call: the first `n_low` degrees
@@ -172,9 +172,13 @@ ttg_status ttg_cheb_filter(ttg_op* op, ttg_block* X, int32_t m, double a, double
  * nonlocal MatMatMults of main.cc:1066-1092. */
 ttg_status ttg_apply_h(ttg_op* op, const ttg_block* X, ttg_block* HX);
 
-/* S = X^T Y (k x k, column-major), FP64.  Replaces MultTM::mult
- * (eigensolver/MultTm.h:37, eigensolver/MultTm.cu:86-224).  s_host may be
- * NULL when only the device copy is wanted (kept inside the op). */
+/* S = X^T Y (k x k, column-major).  Replaces MultTM::mult
+ * (eigensolver/MultTm.h:37, eigensolver/MultTm.cu:86-224).  FP64 data and
+ * result; the products and sums run in double-FP32 arithmetic (each value a
+ * pair of floats, about 47 significant bits, FP32 exponent range): an entry
+ * lands within ~6e-14 of the sum of |terms| of its dot product, where native
+ * FP64 would reach ~1e-16 x length.  s_host may be NULL when only the device
+ * copy is wanted (kept inside the op). */
 ttg_status ttg_gram(ttg_op* op, const ttg_block* X, const ttg_block* Y, double* s_host);
 
 /* S = X^T Y like ttg_gram, for callers that cannot allocate device memory
@@ -184,15 +188,25 @@ ttg_status ttg_gram(ttg_op* op, const ttg_block* X, const ttg_block* Y, double* 
  * dimension ld; S is a device pointer, k x k column-major; stream may be NULL.
  * Allocates nothing: the split-row partial sums live in a fixed 16 MiB
  * __device__ array that every GPU loading this library holds until exit, so
- * k*k must not exceed 2,097,152 (k <= 1448), else TTG_BAD_ARG.  The first call
- * on a device looks up that array's address and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * k*k must not exceed 2,097,152 (k <= 1448), else TTG_BAD_ARG.  Arithmetic as
+ * ttg_gram (double-FP32, about 47 bits).  The first call on a device looks up
+ * the array's address (with lazy module loading this also loads the library's
+ * device code and commits the array), so make it at start-up, before any
+ * stream capture and before the host's no-allocation phase begins.  The
+ * address is cached per device for the life of the process: after a
+ * cudaDeviceReset of that device, do not call this entry point on it again.
+ * All calls share the array: calls that overlap on the GPU race. */
 ttg_status ttg_gram_noalloc(const double* x_dev, const double* y_dev, int64_t n, int32_t k,
                             int64_t ld, double* s_dev, void* stream);
 
-/* Cholesky-QR in FP64: S = X^T X = L L^T, X <- X L^-T.  Replaces MultTM::orth
- * (eigensolver/MultTm.h:39, eigensolver/MultTm.cu:226-467).  Returns
- * TTG_NOT_SPD (X untouched) when S is not numerically positive definite. */
+/* Cholesky-QR: S = X^T X = L L^T, X <- X L^-T.  Replaces MultTM::orth
+ * (eigensolver/MultTm.h:39, eigensolver/MultTm.cu:226-467).  The Gram matrix
+ * S and the product X L^-T are double-FP32 (about 47 bits, see ttg_gram); the
+ * Cholesky factorisation and L^-1 are FP64.  Orthogonality therefore degrades
+ * at condition numbers of X roughly 8x smaller than with native FP64 (the
+ * orthogonality error grows as cond(X)^2 times the Gram's relative error).
+ * Returns TTG_NOT_SPD (X untouched) when S is not numerically positive
+ * definite. */
 ttg_status ttg_chol_qr(ttg_op* op, ttg_block* X);
 
 /* Symmetric eigendecomposition of a k x k column-major FP64 matrix, ascending

@@ -1,5 +1,5 @@
 """The allocation-free Gram entry point (ttg_gram_noalloc), called through the
-C ABI by a caller that owns all device memory, against ttg_gram.
+C ABI by a caller that owns all device memory, against NumPy's X^T Y.
 
 Callers such as memory-pool owners or plugins that may not call cudaMalloc
 hand in their own device buffers; the entry point keeps its partial sums in a
@@ -10,23 +10,21 @@ import ctypes
 import numpy as np
 import pytest
 
-from ttdft_public_gb300 import _lib, api
+from ttdft_public_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
 
-def test_gram_noalloc_matches_gram_on_two_calls_in_a_row(small_system):
+def test_gram_noalloc_matches_numpy_on_two_calls_in_a_row(small_system):
     import torch
 
     s = small_system
     lib = _lib.ttg()
-    op = api.Operator(api.ProjectHamiltonianSparse.from_system(s), 64)
-    mt = api.MultTM()
     rng = np.random.default_rng(31)
     for call, k in enumerate((40, 24)):
         X = rng.standard_normal((s.N, k))
         Y = rng.standard_normal((s.N, k))
-        ref = mt.mult(api.Mat(op, k, X), api.Mat(op, k, Y))
+        ref = X.T @ Y
         # caller-owned device buffers: row-major n x k (ld = k) in, k x k column-major out
         xd = torch.from_numpy(np.ascontiguousarray(X)).cuda()
         yd = torch.from_numpy(np.ascontiguousarray(Y)).cuda()
@@ -36,9 +34,8 @@ def test_gram_noalloc_matches_gram_on_two_calls_in_a_row(small_system):
         assert rc == 0, f"call {call}: status {rc}"
         torch.cuda.synchronize()
         got = sd.cpu().numpy().T            # column-major k x k
-        # same FP64 kernel, same tolerance as the Gram parity test
+        # the Gram parity test's tolerance: 1e-13 of the largest entry
         assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max(), f"call {call}"
-    op.close()
 
 
 def test_gram_noalloc_rejects_sizes_beyond_its_scratch():

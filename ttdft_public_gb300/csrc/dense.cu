@@ -800,8 +800,12 @@ ttg_status fermi(ttg_op* op, const double* eig, int k, double ne, double kT, int
 // it and must be serialised by the caller.
 // The host cannot use the array's name as a device address, so the first call
 // on each device looks the address up with cudaGetSymbolAddress (with that
-// device current) and caches it; that first call should come before any
-// stream capture.
+// device current) and caches it.  With lazy module loading that lookup also
+// loads this library's device code and commits the array, so the first call
+// belongs at start-up, before any stream capture and before the caller's
+// no-allocation phase.  The cache lives as long as the process: a
+// cudaDeviceReset of the device invalidates it, and this entry point must
+// not be called on that device afterwards.
 namespace {
 
 constexpr int64_t kNoAllocScratchDoubles = 2 * 1024 * 1024;

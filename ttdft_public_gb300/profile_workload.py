@@ -25,7 +25,7 @@ from ttdft_public_gb300 import api, system  # noqa: E402
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="atoms64", choices=sorted(system.CONFIGS))
+    ap.add_argument("--workload", default="atoms8", choices=sorted(system.CONFIGS))
     ap.add_argument("--prec", default="fp32,bf16")
     ap.add_argument("--degrees", type=int, default=1)
     ap.add_argument("--rr", action="store_true")

@@ -199,9 +199,11 @@ class Scf:
         return out
 
     def sthosvd(self, field, dims, eps, cap):
-        """Tucker decomposition on the device; returns (core, [U_d]) on host."""
+        """Tucker decomposition on the device; returns (core, [U_d]) on host.
+        cap: one rank cap for all directions, or one per direction."""
         torch = self.torch
-        caps = np.array([min(cap, int(d)) for d in dims], np.int32)
+        cap3 = list(cap) if np.ndim(cap) else [cap] * 3
+        caps = np.array([min(int(c), int(d)) for c, d in zip(cap3, dims)], np.int32)
         core = torch.zeros(int(np.prod(caps)), dtype=torch.float64, device=self.dev)
         U = [torch.zeros(int(dims[d]) * int(caps[d]), dtype=torch.float64, device=self.dev)
              for d in range(3)]
@@ -443,13 +445,12 @@ class Scf:
     def write_density(self, dirpath):
         """write_out_rho (main.cc:1528-1632): the last output density on the
         nodes as a Tucker tensor at the reference's output ranks, in its file
-        format (rank_<r>_core, rank_<r>_factor_{x,y,z}).  One rank cap serves
-        all three directions (the largest of the per-direction ranks; they
-        are equal on cubic grids)."""
+        format (rank_<r>_core, rank_<r>_factor_{x,y,z}), each direction at
+        its own output rank (main.cc:1543-1557)."""
         if getattr(self, "rho_nodal", None) is None:
             raise RuntimeError("no output density yet: run an SCF iteration first")
-        cap = max(tucker_io.output_ranks([int(n) for n in self.ndims]))
-        G, U, r = self.sthosvd(self.rho_nodal, self.ndims, 0.0, cap)
+        caps = tucker_io.output_ranks([int(n) for n in self.ndims])
+        G, U, r = self.sthosvd(self.rho_nodal, self.ndims, 0.0, caps)
         return tucker_io.write_density(dirpath, G.reshape(r, order="F"),
                                        [self.s.basis[d].fem.nodes for d in range(3)], U,
                                        [self.s.basis[d].r for d in range(3)])
