@@ -138,7 +138,9 @@ ttg_status ttg_op_elapsed_ms(ttg_op* op, int32_t slot0, int32_t slot1, float* ms
 #define TTG_KT_TC_BF16 2     /* mma.sync BF16 degree */
 #define TTG_KT_ROWGROUP 3    /* CUDA-core row-group degree (any precision) */
 #define TTG_KT_UMMA_BF16 4   /* tcgen05 BF16 degree */
-#define TTG_KT_KINDS 5
+#define TTG_KT_HARTREE 5     /* ttg_hartree_device: factors + three tcgen05 contractions */
+#define TTG_KT_DENSITY 6     /* ttg_density_device: mode products + squared sum */
+#define TTG_KT_KINDS 7
 ttg_status ttg_op_kernel_timing(ttg_op* op, int32_t enable);
 ttg_status ttg_op_kernel_time(ttg_op* op, int32_t kind, double* ms_total, int64_t* launches);
 
@@ -316,13 +318,27 @@ ttg_status ttg_fermi(ttg_op* op, int32_t k, const double* eig_host, double n_ele
  * Uy, Uz (column-major) are the basis values at the nodes.  Output is
  * nx*ny*nz, x fastest, host memory.  Replaces the per-state reconstruction of
  * ProjectHamiltonianSparse::computeRhoOut (dft/ProjectHamiltonianSparse.cc:
- * 1021-1075).  FP32 tensor-core mode products with a 3-term TF32 split,
- * FP32 accumulation of rho. */
+ * 1021-1075).  Runs in chunks of states (the intermediates stay within a
+ * fixed budget, 3 GiB unless TTG_DENSITY_CHUNK_BYTES says otherwise): three
+ * persistent tcgen05 mode products of FP32 operands cut into exact integer
+ * BF16 slices (see ttg_tc_gemm), the last one squaring, weighting and summing
+ * over the chunk's states in double-FP32 inside its epilogue, so the
+ * orbitals on the grid are never written to memory; rho is FP64. */
 ttg_status ttg_density(ttg_op* op, const ttg_block* X, const double* occ_host,
                        int32_t rx, int32_t ry, int32_t rz,
                        int32_t nx, int32_t ny, int32_t nz,
                        const double* ux, const double* uy, const double* uz,
                        double* rho_host);
+/* ttg_density on device data, on the op's stream, into the op's grow-only
+ * work buffers (no host copy of rho, no synchronisation; a bounded-wait
+ * timeout is reported by ttg_op_sync).  ranks = (rx, ry, rz), n = (nx, ny,
+ * nz): host arrays; u*_dev: FP64 nodal basis values, n_d x r_d column-major;
+ * rho_dev: FP64, nx*ny*nz, x fastest, overwritten (added to when
+ * accumulate). */
+ttg_status ttg_density_device(ttg_op* op, const ttg_block* X, const double* occ_host,
+                              const int32_t* ranks, const int32_t* n, const double* ux_dev,
+                              const double* uy_dev, const double* uz_dev, double* rho_dev,
+                              int32_t accumulate);
 
 /* Hartree potential by the Gaussian kernel expansion
  *   V(i,j,l) = sum_t w_t sum_abc G_abc Fx_t[i,a] Fy_t[j,b] Fz_t[l,c]
@@ -332,9 +348,14 @@ ttg_status ttg_density(ttg_op* op, const ttg_block* X, const double* occ_host,
  * column-major values of the density's Tucker factors at the quadrature
  * points xq with weights wq (J*w); the target grid is x (nx points).
  * alpha and omega are the already-scaled expansion coefficients.
- * All K terms run in one persistent launch on the tensor cores with a 3-term
- * TF32 split (FP32 accuracy); output nx*ny*nz, x fastest, host memory.
- * Needs no op (creates its own stream); device memory is released on return. */
+ * The factor integrals run in FP64 on the CUDA cores (one launch per
+ * direction); the three mode products are persistent tcgen05 launches of
+ * FP32 operands cut into exact integer BF16 slices (see ttg_tc_gemm), the
+ * last one summing the K terms in double-FP32, one group per term, so the
+ * error is that of the FP32 operands whatever K.  Output nx*ny*nz, x
+ * fastest, FP64, host memory.  kernel_ms: device time of the three
+ * contractions.  Needs no op (creates its own stream); device memory is
+ * released on return. */
 ttg_status ttg_hartree(int32_t K, const double* alpha, const double* omega,
                        int32_t rx, int32_t ry, int32_t rz, const double* G,
                        int32_t nqx, int32_t nqy, int32_t nqz,
@@ -344,6 +365,35 @@ ttg_status ttg_hartree(int32_t K, const double* alpha, const double* omega,
                        int32_t nx, int32_t ny, int32_t nz,
                        const double* x, const double* y, const double* z,
                        double* v_host, float* kernel_ms);
+
+/* ttg_hartree on device data, on the op's stream, into the op's grow-only
+ * work buffers (no allocation once they have grown, no host copy, no
+ * synchronisation; a bounded-wait timeout is reported by ttg_op_sync).
+ * alpha_dev, omega_dev: K values; ranks, nq, n: host arrays of 3; g_dev: the
+ * core, x fastest; xq_dev[d], wq_dev[d]: nq[d] quadrature points and J*w
+ * weights; u_dev[d]: nq[d] x ranks[d] column-major; x_dev[d]: n[d] target
+ * points; v_dev: n0*n1*n2 FP64, x fastest.  Same replacement and arithmetic
+ * as ttg_hartree. */
+ttg_status ttg_hartree_device(ttg_op* op, int32_t K, const double* alpha_dev,
+                              const double* omega_dev, const int32_t* ranks, const double* g_dev,
+                              const int32_t* nq, const double* const* xq_dev,
+                              const double* const* wq_dev, const double* const* u_dev,
+                              const int32_t* n, const double* const* x_dev, double* v_dev);
+
+/* C = A B^T on the tensor cores, FP32 operands, FP64 result: A (m x k) and B
+ * (n x k) row-major with leading dimensions lda, ldb (multiples of 4, base
+ * addresses 16-byte aligned), C (m x n) row-major with leading dimension ldc.
+ * The K range is cut into `groups` groups of equal whole 16-value chunks (at
+ * most 192 values each); each group's operands are cut into three integer
+ * BF16 slices on a grid set by the group's largest |value|, their products
+ * accumulate exactly in tensor memory (integer-valued operands come out
+ * exact), and the groups are summed in double-FP32.  The contraction engine
+ * of ttg_hartree and ttg_density, exposed for tests and as a library GEMM;
+ * no counterpart in the reference.  Allocates a few bytes of scratch;
+ * synchronises the stream. */
+ttg_status ttg_tc_gemm(int64_t m, int64_t n, int64_t k, const float* a_dev, int64_t lda,
+                       const float* b_dev, int64_t ldb, int32_t groups, double* c_dev,
+                       int64_t ldc, void* stream);
 
 /* Hartree energy of a Tucker density on its own quadrature grid,
  *   E_H = 1/2 sum_q sum_q' w_q rho_q K(q, q') w_q' rho_q'

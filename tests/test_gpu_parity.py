@@ -308,10 +308,13 @@ def hartree_case(seed=0, r=(12, 10, 8), nq=(40, 36, 30), n=(33, 31, 29), K=7):
 
 
 def test_hartree_matches_oracle():
+    """Random core and factors (heavy cancellation: V ~ 100 from O(1) terms).
+    Rounding the inputs and intermediates to FP32 alone moves V by 6e-8
+    relative here; the tensor-core path measures ~1.3e-7."""
     args = hartree_case()
     V, ms = api.hartree(*args)
     ref = oracle.hartree(*args)
-    assert np.linalg.norm(V - ref) / np.linalg.norm(ref) < 1e-6
+    assert np.linalg.norm(V - ref) / np.linalg.norm(ref) < 3e-7
 
 
 def write_driver_input(path, s, k, m, passes, X0, a_init=0.0, lanczos=20):

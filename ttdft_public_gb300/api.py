@@ -113,7 +113,8 @@ class Operator:
         return ms.value
 
     # kinds of ttg_op_kernel_time (include/ttg.h TTG_KT_*)
-    KERNEL_KINDS = {"umma_fp32": 0, "tc_fp32": 1, "tc_bf16": 2, "rowgroup": 3, "umma_bf16": 4}
+    KERNEL_KINDS = {"umma_fp32": 0, "tc_fp32": 1, "tc_bf16": 2, "rowgroup": 3, "umma_bf16": 4,
+                    "hartree": 5, "density": 6}
 
     def kernel_timing(self, enable: bool):
         """Bracket every fused filter-degree launch with CUDA events on the

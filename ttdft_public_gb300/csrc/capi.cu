@@ -274,7 +274,8 @@ ttg_status ttg_op_set_rr_precision(ttg_op* op, int32_t prec) {
 ttg_status ttg_op_sync(ttg_op* op) {
   if (!op) return TTG_BAD_ARG;
   TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
-  return umma_check_error(op);
+  TTG_TRY(umma_check_error(op));
+  return hartree_error(op);
 }
 
 ttg_status ttg_op_record(ttg_op* op, int32_t slot) {

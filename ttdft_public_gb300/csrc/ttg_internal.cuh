@@ -157,6 +157,28 @@ struct KernelTimer {
   long long count[TTG_KT_KINDS] = {};
 };
 
+// Work buffers of the Hartree kernel expansion (tensor.cu), grow-only and
+// owned by the operator, so the SCF's calls allocate nothing once warm.
+struct HartreeWork {
+  DevBuf F[3];     // FP32 expansion factors (x, y: [t][i][a]; z: [l][t, c] with the weight)
+  DevBuf gf;       // FP32 core, rows (b, c), a contiguous
+  DevBuf p2;       // FP32 [t][(i, c)][b]
+  DevBuf q;        // FP32 [(i, j)][(t, c)]
+  int64_t q_layout[3] = {0, 0, 0};   // (rows, K, padded rank) the zeroed Q was laid out for
+  DevBuf amax;     // FP32 group maxima of the operands (the tensor-core slicing grid)
+  DevBuf err;      // int: a bounded wait of the tensor-core kernel ran out
+};
+
+// Work buffers of the density build (tensor.cu), grow-only, owned by the op.
+struct DensityWork {
+  DevBuf uf[3];    // FP32 basis values at the nodes, [i][a] (row stride a multiple of 4)
+  DevBuf xt;       // FP32 block chunk, [s][(b, c)][a]
+  DevBuf p1;       // FP32 [s][c][i][b]
+  DevBuf p2;       // FP32 [s][j][i][c]
+  DevBuf w;        // FP32 weights 2 f_s
+  DevBuf amax;     // FP32 group maxima of the operands (the tensor-core slicing grid)
+};
+
 struct Csr {
   int64_t rows = 0, cols = 0, nnz = 0, max_row_nnz = 0;
   DevBuf ptr;      // int64
@@ -199,6 +221,9 @@ struct ttg_op {
   ttg::DevBuf status;         // int32 device status words
   cudaEvent_t ev[ttg::kMaxSlots] = {};
   ttg::KernelTimer kt;
+  ttg::HartreeWork hw;        // Hartree work buffers (ttg_hartree_device) and the
+                              // tensor-core error word shared with the density
+  ttg::DensityWork dw;        // density work buffers (ttg_density_device)
   int64_t launches = 0;
   int64_t device_bytes = 0;
 };
@@ -241,6 +266,10 @@ ttg_status launch_cheb_tc(ttg_op* op, int prec, const void* src, const void* xol
                           int k, double alpha, double beta, double delta);
 ttg_status launch_convert(ttg_op* op, int from, int to, const void* src, void* dst,
                           int64_t rows, int k);
+
+// tensor.cu: TTG_TIMEOUT (and clears the word) when a tensor-core launch of
+// ttg_hartree_device or ttg_density_device gave up a bounded wait
+ttg_status hartree_error(ttg_op* op);
 
 // scf.cu: FP64 strided-batched GEMM (split-K when the output is small)
 #ifdef __CUDACC__

@@ -129,13 +129,20 @@ class Scf:
         self.nq = int(np.prod(self.q))
         H = api.ProjectHamiltonianSparse.from_system(sysm)
         self.op = api.Operator(H, self.k)
+        # every grid call runs on the operator's stream, in order with the
+        # asynchronous Hartree and density launches
+        self.st = ctypes.c_void_p(self.op.stream())
         mats = [bb.stiffness() for bb in b] + [bb.overlap() for bb in b]
         mats = [np.ascontiguousarray(m_) for m_ in mats]
         check(self.lib.ttg_op_set_kinetic(self.op.h, *[_lib.ptr(m_) for m_ in mats]),
               "ttg_op_set_kinetic")
         self.wq = [self._dev(bb.fem.wJ) for bb in b]
         self.xq = [bb.fem.xq for bb in b]
+        self.xq_dev = [self._dev(x) for x in self.xq]
         self.alpha, self.omega = coulomb_expansion()
+        self.alpha_dev, self.omega_dev = self._dev(self.alpha), self._dev(self.omega)
+        # basis values at the nodes (n_d x r_d column-major) for the density
+        self.unodal_dev = [self._dev(np.asfortranarray(bb.nodal).reshape(-1, order="F")) for bb in b]
         # fixed local potential: Gaussian wells + neutralising ionic charges
         self.vloc = self._zeros()
         fx = [np.stack([np.exp(-(self.xq[d] - a[d]) ** 2 / (2 * spec.sigma ** 2)) for a in sysm.atoms])
@@ -145,7 +152,7 @@ class Scf:
         zs = self._dev(np.full(self.natoms, spec.z_val))
         check(self.lib.ttg_grid_ion_potential(self.natoms, self._p(pos), self._p(zs),
                                               self.cfg.ion_width, *[self._p(self._dev(x)) for x in self.xq],
-                                              _lib.ptr(self.qdims), self._p(self.vloc), None),
+                                              _lib.ptr(self.qdims), self._p(self.vloc), self.st),
               "ttg_grid_ion_potential")
         self.e_nn = repulsive_energy(sysm.atoms, spec.z_val)
         self.timings = {}
@@ -181,21 +188,21 @@ class Scf:
         c = self._dev(coef)
         fd = [self._dev(np.ascontiguousarray(x)) for x in f]
         check(self.lib.ttg_grid_cp_sum(len(coef), self._p(c), *[self._p(x) for x in fd],
-                                       _lib.ptr(dims), self._p(out), 1 if accumulate else 0, None),
+                                       _lib.ptr(dims), self._p(out), 1 if accumulate else 0, self.st),
               "ttg_grid_cp_sum")
 
     def integrate(self, f, g=None):
         res = ctypes.c_double()
         check(self.lib.ttg_grid_integrate(self._p(f), None if g is None else self._p(g),
                                           _lib.ptr(self.qdims), *[self._p(w) for w in self.wq],
-                                          ctypes.byref(res), None), "ttg_grid_integrate")
+                                          ctypes.byref(res), self.st), "ttg_grid_integrate")
         return res.value
 
     def lincomb(self, fields, coef, out, take_abs=False):
         arr = (ctypes.c_void_p * len(fields))(*[f.data_ptr() for f in fields])
         c = np.ascontiguousarray(coef, dtype=np.float64)
         check(self.lib.ttg_grid_lincomb(len(fields), arr, _lib.ptr(c), out.numel(), self._p(out),
-                                        1 if take_abs else 0, None), "ttg_grid_lincomb")
+                                        1 if take_abs else 0, self.st), "ttg_grid_lincomb")
         return out
 
     def sthosvd(self, field, dims, eps, cap):
@@ -218,12 +225,19 @@ class Scf:
         return G, Uh, r
 
     def hartree(self, G, Uq, r):
-        """V_H on the quadrature grid from a Tucker density with factors at
-        the quad points (one launch over all expansion terms)."""
-        quad = [(self.xq[d], self.fem_w(d)) for d in range(3)]
-        V, ms = api.hartree(self.alpha, self.omega, G.reshape(r[2], r[1], r[0]), quad, Uq, self.xq)
-        self.timings["hartree_ms"] = self.timings.get("hartree_ms", 0.0) + ms
-        return self._dev(V.reshape(-1))
+        """V_H on the quadrature grid (device, FP64) from a Tucker density with
+        factors at the quad points: ttg_hartree_device on the operator's
+        stream, all expansion terms in one tensor-core contraction."""
+        core = self._dev(np.ascontiguousarray(G).reshape(-1))
+        U = [self._dev(np.asfortranarray(Uq[d]).reshape(-1, order="F")) for d in range(3)]
+        V = self._zeros()
+        vp = lambda ts: (ctypes.c_void_p * 3)(*[t.data_ptr() for t in ts])  # noqa: E731
+        check(self.lib.ttg_hartree_device(self.op.h, self.alpha.size, self._p(self.alpha_dev),
+                                          self._p(self.omega_dev), _lib.ptr(np.array(r, np.int32)),
+                                          self._p(core), _lib.ptr(self.qdims), vp(self.xq_dev),
+                                          vp(self.wq), vp(U), _lib.ptr(self.qdims), vp(self.xq_dev),
+                                          self._p(V)), "ttg_hartree_device")
+        return V
 
     def hartree_energy(self, G, Uq, r):
         quad = [(self.xq[d], self.fem_w(d)) for d in range(3)]
@@ -239,7 +253,7 @@ class Scf:
         out = torch.zeros(int(np.prod(dims)), dtype=torch.float64, device=self.dev)
         check(self.lib.ttg_tucker_reconstruct(self._p(core), _lib.ptr(np.array(r, np.int32)),
                                               *[self._p(u) for u in Ud],
-                                              _lib.ptr(np.asarray(dims, np.int32)), self._p(out), None),
+                                              _lib.ptr(np.asarray(dims, np.int32)), self._p(out), self.st),
               "ttg_tucker_reconstruct")
         return out
 
@@ -280,8 +294,8 @@ class Scf:
         cfg = self.cfg
         G, U, r = self.sthosvd(rho_in, self.qdims, cfg.rho_eps, cfg.rho_rank_cap)
         vh = self.hartree(G, U, r)
-        veff = vh + self.vloc
-        check(self.lib.ttg_grid_lda(self._p(rho_in), self.nq, self._p(veff), None, 1, None),
+        veff = self.lincomb([vh, self.vloc], [1.0, 1.0], vh)
+        check(self.lib.ttg_grid_lda(self._p(rho_in), self.nq, self._p(veff), None, 1, self.st),
               "ttg_grid_lda")
         return veff
 
@@ -297,8 +311,12 @@ class Scf:
         """computeRhoOut: nodal density, STHOSVD, factors projected to the
         quadrature points, reconstruction, |.|; also returns the Tucker form
         at the quad points for the Hartree term."""
-        rho_n = api.density(self.op, X, occ, self.s.basis).reshape(-1)
-        rho_nd = self._dev(rho_n)
+        r = np.array([bb.r for bb in self.s.basis], np.int32)
+        rho_nd = self._zeros(int(np.prod(self.ndims)))
+        occ = np.ascontiguousarray(occ, dtype=np.float64)
+        check(self.lib.ttg_density_device(self.op.h, X.h, _lib.ptr(occ), _lib.ptr(r),
+                                          _lib.ptr(self.ndims), *[self._p(u) for u in self.unodal_dev],
+                                          self._p(rho_nd), 0), "ttg_density_device")
         self.rho_nodal = rho_nd
         G, U, r = self.sthosvd(rho_nd, self.ndims, self.cfg.rho_out_eps, self.cfg.rho_out_rank_cap)
         Uq = [self.s.basis[d].fem.interp_matrix() @ U[d] for d in range(3)]
@@ -399,7 +417,7 @@ class Scf:
             # energy (main.cc:1315-1401)
             e_band = float(np.sum(2.0 * occ * w))
             exc = self._zeros()
-            check(self.lib.ttg_grid_lda(self._p(rho_out), self.nq, None, self._p(exc), 0, None),
+            check(self.lib.ttg_grid_lda(self._p(rho_out), self.nq, None, self._p(exc), 0, self.st),
                   "ttg_grid_lda")
             e_grid = (self.integrate(exc) + e_h
                       - self.integrate(rho_out, veff) + self.integrate(rho_out, self.vloc))
