@@ -15,32 +15,34 @@
 // Instead, every operand value v of a group (or batch) with max |v| < 2^e is
 // cut into three integer slices on a common grid,
 //   v 2^(8-e) = a0 + a1 2^-8 + a2 2^-16 + O(2^-17),  a_p integers, |a_p| <= 256,
-// which BF16 holds exactly.  Products of slices are exact integers, and the
-// sums of one level L = p + q (a0b0; a0b1 + a1b0; a0b2 + a1b1 + a2b0) stay
-// below 2^24 for a group of up to 192 K values, so each level accumulates in
-// its own tensor-memory accumulator without rounding (integer-valued operands
-// come out exact).  The epilogue adds S0 + S1 2^-8 + S2 2^-16 with
-// error-free two-sums (the levels can cancel), scales by 2^(eA + eB - 16)
-// and sums the groups in double-FP32: the result carries the operands' FP32
-// quantisation (2^-25 of each group's largest value) and nothing else.  The
-// group maxima come from the kernels that write the operands (atomicMax on
-// |v|).
+// which BF16 holds exactly.  Products of slices are exact integers; the sums
+// of one level L = p + q (a0b0; a0b1 + a1b0; a0b2 + a1b1 + a2b0; a1b2 + a2b1)
+// stay below 2^24 for a group of up to 192 K values, so each level
+// accumulates in its own tensor-memory accumulator without rounding
+// (integer-valued operands come out exact); only a2b2, 2^-32 of the leading
+// product, is left out.  The epilogue adds S0 + S1 2^-8 + S2 2^-16 + S3 2^-24
+// with error-free two-sums (the levels can cancel), scales by
+// 2^(eA + eB - 16) and sums the groups in double-FP32: the result carries the
+// operands' FP32 quantisation (2^-25 of each group's largest value) and
+// nothing else.  The group maxima come from the kernels that write the
+// operands (atomicMax on |v|).
 //
-// Data movement (one CTA per SM, persistent over output tiles of 128 x 64):
+// Data movement (one CTA per SM, persistent over output tiles of 128 x 48):
 //  - warp 0, one thread: TMA tiled loads (cp.async.bulk.tensor) of the FP32
-//    tiles A[128 rows][16] and B[64 rows][16] of one K-chunk into a raw
+//    tiles A[128 rows][16] and B[48 rows][16] of one K-chunk into a raw
 //    ring; rows and K beyond the tensor's extent are filled with zeros;
-//  - warps 4-9 (one thread per row): slice the raw tiles into three BF16
-//    planes each, written in the canonical K-major layout of the MMA operands
-//    (8-row x 16-byte core matrices), fence them for the async proxy, arrive;
+//  - warps 4-9, whole chunks in turn: slice the chunk's 176 rows into three
+//    BF16 planes each, written in the canonical K-major layout of the MMA
+//    operands (8-row x 16-byte core matrices), fence them for the async
+//    proxy, arrive;
 //  - warp 2, one thread: waits for each chunk's slices (and, at the start of
 //    a group, for the epilogue to have emptied the accumulators the group
 //    will use) and publishes the count of ready chunks;
-//  - warp 1, one thread: six MMAs (M128 N64 K16) per chunk into the three
+//  - warp 1, one thread: eight MMAs (M128 N48 K16) per chunk into the four
 //    level accumulators of one of two buffers (double-buffered across
 //    groups), a commit per chunk to free the slice stage and per group to
 //    hand the buffer to the epilogue;
-//  - warps 10-17 (two per 32 TMEM lanes, 32 columns each): combine the levels
+//  - warps 10-17 (two per 32 TMEM lanes, 24 columns each): combine the levels
 //    and store (one group: FP32, with the output's per-batch max |v| for the
 //    next contraction) or add into hi/lo sums kept in tensor memory after the
 //    two buffers, stored as FP64 after the last group.
@@ -60,22 +62,23 @@ namespace ttg {
 namespace {
 
 constexpr int TG_M = 128;                         // rows of an A tile (MMA M)
-constexpr int TG_N = 64;                          // rows of a B tile (MMA N)
+constexpr int TG_N = 48;                          // rows of a B tile (MMA N)
 constexpr int TG_K = 16;                          // K per chunk (one MMA)
 constexpr int kRawA = TG_M * TG_K * 4;            // 8 KB FP32
-constexpr int kRawB = TG_N * TG_K * 4;            // 4 KB FP32
-constexpr int kRawStage = kRawA + kRawB;
+constexpr int kRawB = TG_N * TG_K * 4;            // 3 KB FP32
+constexpr int kRawStage = kRawA + kRawB;          // 11 KB (a multiple of 1 KB: TMA destinations)
 constexpr int kPlaneA = TG_M * TG_K * 2;          // 4 KB: one BF16 slice plane of A
-constexpr int kPlaneB = TG_N * TG_K * 2;          // 2 KB
-constexpr int kSplitStage = 3 * kPlaneA + 3 * kPlaneB;   // 18 KB
-constexpr int kRawStages = 6;
-constexpr int kSplitStages = 6;
+constexpr int kPlaneB = TG_N * TG_K * 2;          // 1.5 KB
+constexpr int kSplitStage = 3 * kPlaneA + 3 * kPlaneB;   // 16.5 KB
+constexpr int kRawStages = 8;
+constexpr int kSplitStages = 7;
 constexpr int kSmem = kRawStages * kRawStage + kSplitStages * kSplitStage + 1024;
-constexpr int kConvWarp0 = 4, kConvWarps = 6;     // one thread per row: 128 A + 64 B rows
+constexpr int kConvWarp0 = 4, kConvWarps = 6;     // whole chunks in turn (<= kSplitStages)
+constexpr int kRows = TG_M + TG_N;                // rows a converter warp slices per chunk
 constexpr int kEpiWarp0 = 10, kEpiWarps = 8;      // two warps per 32 TMEM lanes
 constexpr int kThreads = (kEpiWarp0 + kEpiWarps) * 32;   // 576
-constexpr int kBufCols = 3 * TG_N;                // three level accumulators per buffer
-constexpr uint32_t kTmemCols = 512;               // 2 buffers (384) + hi, lo (128)
+constexpr int kBufCols = 4 * TG_N;                // four level accumulators per buffer
+constexpr uint32_t kTmemCols = 512;               // 2 buffers (384) + hi, lo (96)
 constexpr int kMaxWait = 1 << 22;
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
@@ -93,7 +96,7 @@ __device__ __forceinline__ uint64_t kmajor_desc(uint32_t addr) {
   return d;
 }
 
-// kind::f16: BF16 x BF16 -> FP32, A and B K-major, M = 128, N = 64
+// kind::f16: BF16 x BF16 -> FP32, A and B K-major, M = 128, N = 48
 __device__ __forceinline__ uint32_t idesc_mma() {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TG_N >> 3) << 17) |
          ((uint32_t)(TG_M >> 4) << 24);
@@ -261,10 +264,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
   if (tid == 32) {
     for (int s = 0; s < kRawStages; ++s) {
       bar_init(&raw_full[s], 1);
-      bar_init(&raw_empty[s], kConvWarps);
+      bar_init(&raw_empty[s], 1);
     }
     for (int s = 0; s < kSplitStages; ++s) {
-      bar_init(&spl_full[s], kConvWarps);
+      bar_init(&spl_full[s], 1);
       bar_init(&spl_empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -314,54 +317,55 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
           bar_drain(&raw_full[r % kRawStages], (uint32_t)((r / kRawStages) & 1));
     }
   } else if (warp >= kConvWarp0 && warp < kConvWarp0 + kConvWarps) {
-    // ---- slice FP32 rows into three integer BF16 planes (row ct of A, or of B)
-    const int ct = tid - kConvWarp0 * 32;            // 0..191
-    const bool isb = ct >= TG_M;
-    const int row = isb ? ct - TG_M : ct;
-    const float* amax = isb ? amaxB : amaxA;
-    int64_t q = 0;
-    for (int j = 0; j < my_tiles && ok; ++j) {
+    // ---- slice whole chunks, chunk q to converter warp q % kConvWarps: the 128 A
+    // rows and 48 B rows of a chunk into three integer BF16 planes each
+    const int cw = warp - kConvWarp0;
+    const int64_t total = (int64_t)my_tiles * nk;
+    for (int64_t q = cw; q < total; q += kConvWarps) {
+      const int j = (int)(q / nk), c = (int)(q % nk);
       int tm, tn, z;
       sch.at(blockIdx.x + (int64_t)j * gridDim.x, tm, tn, z);
-      for (int c = 0; c < nk; ++c, ++q) {
-        const int s = (int)(q % kRawStages), s2 = (int)(q % kSplitStages);
-        const int g = c / kg;
-        const int e = grid_exp(__ldg(amax + (isb ? sidx_b(g, z) : sidx_a(g, z))));
-        const float sc = ldexpf(1.f, 8 - e);
-        bool w = true;
-        if (lane == 0) w = bar_wait(&raw_full[s], (uint32_t)((q / kRawStages) & 1), abrt, 0);
-        w = __shfl_sync(0xffffffffu, w, 0);
-        if (!w) { ok = false; break; }
+      const int s = (int)(q % kRawStages), s2 = (int)(q % kSplitStages);
+      const int g = c / kg;
+      const float sca = ldexpf(1.f, 8 - grid_exp(__ldg(amaxA + sidx_a(g, z))));
+      const float scb = ldexpf(1.f, 8 - grid_exp(__ldg(amaxB + sidx_b(g, z))));
+      bool w = true;
+      if (lane == 0) {
+        w = bar_wait(&raw_full[s], (uint32_t)((q / kRawStages) & 1), abrt, 0);
+        // the MMAs of chunk q - kSplitStages have read this slice stage
+        if (w && q >= kSplitStages)
+          w = bar_wait(&spl_empty[s2], (uint32_t)((q / kSplitStages - 1) & 1), abrt, 0);
+      }
+      w = __shfl_sync(0xffffffffu, w, 0);
+      if (!w) { ok = false; break; }
+      const unsigned char* src0 = raw + s * kRawStage;
+      unsigned char* dst0 = spl + s2 * kSplitStage;
+      for (int r = lane; r < kRows; r += 32) {
+        const bool isb = r >= TG_M;
+        const int row = isb ? r - TG_M : r;
         float v[16];
-        const float4* src = reinterpret_cast<const float4*>(raw + s * kRawStage +
-                                                            (isb ? kRawA : 0) + row * 64);
+        const float4* src = reinterpret_cast<const float4*>(src0 + (isb ? kRawA : 0) + row * 64);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const float4 f = src[i];
           v[4 * i] = f.x; v[4 * i + 1] = f.y; v[4 * i + 2] = f.z; v[4 * i + 3] = f.w;
         }
-        __syncwarp();
-        if (lane == 0) bar_arrive(&raw_empty[s]);
-        if (q >= kSplitStages) {
-          if (lane == 0)
-            w = bar_wait(&spl_empty[s2], (uint32_t)((q / kSplitStages - 1) & 1), abrt, 0);
-          w = __shfl_sync(0xffffffffu, w, 0);
-          if (!w) { ok = false; break; }
-        }
         const int plane = isb ? kPlaneB : kPlaneA;
-        unsigned char* dst = spl + s2 * kSplitStage + (isb ? 3 * kPlaneA : 0) + (row >> 3) * 256 +
-                             (row & 7) * 16;
+        unsigned char* dst = dst0 + (isb ? 3 * kPlaneA : 0) + (row >> 3) * 256 + (row & 7) * 16;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           uint4 p0, p1, p2;
-          slice8(v + 8 * h, sc, p0, p1, p2);
+          slice8(v + 8 * h, isb ? scb : sca, p0, p1, p2);
           *reinterpret_cast<uint4*>(dst + h * 128) = p0;
           *reinterpret_cast<uint4*>(dst + plane + h * 128) = p1;
           *reinterpret_cast<uint4*>(dst + 2 * plane + h * 128) = p2;
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncwarp();
-        if (lane == 0) bar_arrive(&spl_full[s2]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) {
+        bar_arrive(&raw_empty[s]);
+        bar_arrive(&spl_full[s2]);
       }
     }
   } else if (warp == 2) {
@@ -392,9 +396,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
       const uint32_t spl0 = su32(spl);
       int64_t q = 0, gg = 0;
       uint32_t avail = 0;
-      // (slice of A, slice of B, level): level 2 first, then 1, then 0
-      const int ta[6] = {1, 0, 2, 0, 1, 0}, tb[6] = {1, 2, 0, 1, 0, 0}, lv[6] = {2, 2, 2, 1, 1, 0};
-      const bool first[6] = {true, false, false, true, false, true};
+      // (slice of A, slice of B, level): level 3 first, then 2, 1, 0; the level-4
+      // product a2 b2 (2^-32 of the leading one) is left out
+      const int ta[8] = {1, 2, 1, 0, 2, 0, 1, 0}, tb[8] = {2, 1, 1, 2, 0, 1, 0, 0};
+      const int lv[8] = {3, 3, 2, 2, 2, 1, 1, 0};
+      const bool first[8] = {true, false, true, false, false, true, false, true};
       for (int j = 0; j < my_tiles && ok; ++j)
         for (int g = 0; g < G && ok; ++g, ++gg) {
           const uint32_t dbuf = tmem + (uint32_t)((gg & 1) * kBufCols);
@@ -408,7 +414,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t base = spl0 + (uint32_t)((q % kSplitStages) * kSplitStage);
 #pragma unroll
-            for (int p = 0; p < 6; ++p) {
+            for (int p = 0; p < 8; ++p) {
               const uint64_t da = kmajor_desc(base + ta[p] * kPlaneA);
               const uint64_t db = kmajor_desc(base + 3 * kPlaneA + tb[p] * kPlaneB);
               const uint32_t acc = (c > 0 || !first[p]) ? 1u : 0u;
@@ -434,7 +440,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
       bar_drain(&fin, 0);
     }
   } else if (warp >= kEpiWarp0) {
-    // ---- epilogue: TMEM lanes 32 (warp & 3) .., columns 32 half .. 32 half + 31
+    // ---- epilogue: TMEM lanes 32 (warp & 3) .., columns 24 half .. 24 half + 23
     const int qd = warp & 3, half = (warp - kEpiWarp0) >> 2;
     const int row = qd * 32 + lane;
     const uint32_t lanes = (uint32_t)(qd * 32) << 16;
@@ -445,10 +451,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
       const int64_t m = (int64_t)tm * TG_M + row;
       const bool mok = m < M;
       const int64_t base = mok ? (m % out.r1) * out.s1 + (m / out.r1) * out.s2 + z * out.bs : 0;
-      const int n0 = tn * TG_N + half * 32;
+      const int n0 = tn * TG_N + half * (TG_N / 2);
       // running double-FP32 sums of the groups (TG_SUM_F64, TG_SQSUM_F64) in
       // tensor memory after the two accumulator buffers: hi, then lo
-      const uint32_t hcol = tmem + lanes + (uint32_t)(2 * kBufCols + half * 32);
+      const uint32_t hcol = tmem + lanes + (uint32_t)(2 * kBufCols + half * (TG_N / 2));
       const uint32_t lcol = hcol + (uint32_t)TG_N;
       float vmax = 0.f;
       for (int g = 0; g < G; ++g, ++gg) {
@@ -458,26 +464,30 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
         const float scale = ldexpf(1.f, grid_exp(__ldg(amaxA + sidx_a(g, z))) +
                                             grid_exp(__ldg(amaxB + sidx_b(g, z))) - 16);
         const float wg = MODE == TG_SQSUM_F64 ? __ldg(out.w + g) : 0.f;
-        const uint32_t acol = tmem + lanes + (uint32_t)((gg & 1) * kBufCols + half * 32);
+        const uint32_t acol = tmem + lanes + (uint32_t)((gg & 1) * kBufCols + half * (TG_N / 2));
 #pragma unroll
-        for (int c0 = 0; c0 < 32; c0 += 8) {
-          float s0[8], s1[8], s2[8];
+        for (int c0 = 0; c0 < TG_N / 2; c0 += 8) {
+          float s0[8], s1[8], s2[8], s3[8];
           tmem_ld8(acol + c0, s0);
           tmem_ld8(acol + TG_N + c0, s1);
           tmem_ld8(acol + 2 * TG_N + c0, s2);
-          // the group's value S0 + S1 2^-8 + S2 2^-16 as an unevaluated pair
-          // (vh, vl): the level sums are exact integers and partly cancel, so
-          // they are added with error-free two-sums, not rounded in FP32
+          tmem_ld8(acol + 3 * TG_N + c0, s3);
+          // the group's value S0 + S1 2^-8 + S2 2^-16 + S3 2^-24 as an
+          // unevaluated pair (vh, vl): the level sums are exact integers and
+          // partly cancel, so they are added with error-free two-sums
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const float t1 = s1[i] * (1.f / 256.f), t2 = s2[i] * (1.f / 65536.f);
-            const float h = s0[i] + t1;
-            float bv = h - s0[i];
-            float l = (s0[i] - (h - bv)) + (t1 - bv);
-            const float h2 = h + t2;
-            bv = h2 - h;
-            l += (h - (h2 - bv)) + (t2 - bv);
-            float vh = h2 * scale, vl = l * scale;
+            const float t[3] = {s1[i] * (1.f / 256.f), s2[i] * (1.f / 65536.f),
+                                s3[i] * (1.f / 16777216.f)};
+            float h = s0[i], l = 0.f;
+#pragma unroll
+            for (int u = 0; u < 3; ++u) {
+              const float h2 = h + t[u];
+              const float bv = h2 - h;
+              l += (h - (h2 - bv)) + (t[u] - bv);
+              h = h2;
+            }
+            float vh = h * scale, vl = l * scale;
             if constexpr (MODE == TG_STORE_F32) {
               const float v = vh + vl;
               const int64_t n = n0 + c0 + i;
