@@ -159,30 +159,10 @@ def test_config2_fp64_pass_matches_oracle_and_mixed_converges_to_fp64(atoms64_sy
     op.close()
 
 
-def config3_case(rank=60, n_blobs=64, seed=303, width=1.0):
-    """Configuration 3: a Tucker density with core rank^3 and factors at the 360
-    quadrature points per direction of the 32-bohr, 120-element mesh, taken
-    from 64 seeded Gaussian charge blobs (HOSVD of their sum, computed from the
-    blobs' separable form), the 35-term kernel expansion, output on the
-    quadrature grid."""
-    from ttdft_public_gb300.kernel_expansion import coulomb_expansion
-    fem = system.Fem1D(120, 0.0, 32.0)
-    xq, wq = fem.xq, fem.wJ
-    atoms = system.place_atoms(n_blobs, 32.0, 3.0, 2.5, seed)
-    norm = 1.0 / (np.pi * width * width) ** 1.5
-    g = [np.exp(-(xq[None, :] - atoms[:, d][:, None]) ** 2 / width ** 2) for d in range(3)]
-    U = []
-    for d in range(3):
-        o = [e for e in range(3) if e != d]
-        # mode-d Gram of sum_a norm gx_a (x) gy_a (x) gz_a
-        S = (g[o[0]] @ g[o[0]].T) * (g[o[1]] @ g[o[1]].T) * norm * norm
-        w, V = np.linalg.eigh(g[d].T @ S @ g[d])
-        U.append(V[:, ::-1][:, :rank].copy())
-    P = [U[d].T @ g[d].T for d in range(3)]                  # (rank, n_blobs)
-    G = norm * np.einsum("ia,ja,ka->kji", P[0], P[1], P[2])  # (rz, ry, rx), x fastest
-    alpha, omega = coulomb_expansion()
-    quad = [(xq, wq)] * 3
-    return alpha, omega, G, quad, U, [xq] * 3
+def config3_case(rank=60):
+    """Configuration 3: core 60^3, 360 quadrature points per direction of the
+    32-bohr, 120-element mesh, 64 seeded Gaussian charge blobs, 35 terms."""
+    return system.hartree_blob_case(rank=rank)
 
 
 def test_config3_hartree_35_terms_against_fp64():

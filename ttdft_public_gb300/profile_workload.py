@@ -4,12 +4,14 @@
         --prec fp32,bf16 --degrees 1 [--rr] [--states K]
     python -m ttdft_public_gb300.profile_workload --workload atoms64 --scf 1 \
         [--filter mixed]
+    python -m ttdft_public_gb300.profile_workload --hartree 3
 
 Builds the workload's operator, uploads a random block and runs `degrees`
 filter degrees per listed precision (one fused SpMM launch each) and, with
 --rr, one Rayleigh-Ritz projection (the df64 SpMM, Gram and eigensolve).  Few
 launches and no timing loop, so that an ncu capture of it stays small.  With
---scf N it runs N iterations of the SCF loop instead (for launch lists)."""
+--scf N it runs N iterations of the SCF loop instead (for launch lists),
+with --hartree N N evaluations of the standalone Hartree contraction."""
 from __future__ import annotations
 
 import argparse
@@ -32,7 +34,16 @@ def main():
     ap.add_argument("--scf", type=int, default=0)
     ap.add_argument("--filter", default="mixed", choices=("fp64", "fp32", "mixed"))
     ap.add_argument("--states", type=int, default=0, help="block width (default: the workload's)")
+    ap.add_argument("--hartree", type=int, default=0,
+                    help="instead: N evaluations of the 35-term Hartree contraction on the "
+                         "standalone workload (core 60^3, 360 points per direction)")
     args = ap.parse_args()
+    if args.hartree:
+        case = system.hartree_blob_case()
+        for _ in range(args.hartree):
+            V, ms = api.hartree(*case)
+            print(f"hartree contractions {ms:.3f} ms")
+        return
     s = system.build_system(system.CONFIGS[args.workload],
                             cache_dir=os.environ.get("TTG_CACHE"))
     if args.scf:

@@ -350,3 +350,29 @@ def _load(spec: SystemSpec, path: str) -> KSSystem:
     H = Csr(N, N, z["Hp"], z["Hc"], z["Hv"])
     C = Csr(int(z["Cn"][0]), N, z["Cp"], z["Cc"], z["Cv"])
     return KSSystem(spec, z["atoms"], basis, H, C, z["D"], {})
+
+
+def hartree_blob_case(rank=60, n_blobs=64, seed=303, width=1.0, n_el=120, box=32.0):
+    """The standalone Hartree workload: a Tucker density with core rank^3 and
+    factors at the 3 n_el quadrature points per direction of a box-bohr mesh
+    (360 for 120 elements), from n_blobs seeded Gaussian charge blobs (HOSVD
+    of their sum, computed from the blobs' separable form), the 35-term kernel
+    expansion, output on the quadrature grid.  Returns (alpha, omega, G as
+    (rz, ry, rx), quad = [(xq, wq)] * 3, U = [nq x rank] * 3, grids)."""
+    from .kernel_expansion import coulomb_expansion
+    fem = Fem1D(n_el, 0.0, box)
+    xq, wq = fem.xq, fem.wJ
+    atoms = place_atoms(n_blobs, box, 3.0, 2.5, seed)
+    norm = 1.0 / (math.pi * width * width) ** 1.5
+    g = [np.exp(-(xq[None, :] - atoms[:, d][:, None]) ** 2 / width ** 2) for d in range(3)]
+    U = []
+    for d in range(3):
+        o = [e for e in range(3) if e != d]
+        # mode-d Gram of sum_a norm gx_a (x) gy_a (x) gz_a
+        S = (g[o[0]] @ g[o[0]].T) * (g[o[1]] @ g[o[1]].T) * norm * norm
+        w, V = np.linalg.eigh(g[d].T @ S @ g[d])
+        U.append(V[:, ::-1][:, :rank].copy())
+    P = [U[d].T @ g[d].T for d in range(3)]                  # (rank, n_blobs)
+    G = norm * np.einsum("ia,ja,ka->kji", P[0], P[1], P[2])  # (rz, ry, rx), x fastest
+    alpha, omega = coulomb_expansion()
+    return alpha, omega, G, [(xq, wq)] * 3, U, [xq] * 3
