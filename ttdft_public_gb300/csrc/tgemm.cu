@@ -331,10 +331,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
       const float scb = ldexpf(1.f, 8 - grid_exp(__ldg(amaxB + sidx_b(g, z))));
       bool w = true;
       if (lane == 0) {
-        w = bar_wait(&raw_full[s], (uint32_t)((q / kRawStages) & 1), abrt, 0);
+        w = bar_wait(&raw_full[s], (uint32_t)((q / kRawStages) & 1), abrt, 32);
         // the MMAs of chunk q - kSplitStages have read this slice stage
         if (w && q >= kSplitStages)
-          w = bar_wait(&spl_empty[s2], (uint32_t)((q / kSplitStages - 1) & 1), abrt, 0);
+          w = bar_wait(&spl_empty[s2], (uint32_t)((q / kSplitStages - 1) & 1), abrt, 32);
       }
       w = __shfl_sync(0xffffffffu, w, 0);
       if (!w) { ok = false; break; }
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
               break;
             }
             if (!bar_wait(&spl_full[q % kSplitStages], (uint32_t)((q / kSplitStages) & 1), abrt,
-                          0)) {
+                          16)) {
               ok = false;
               break;
             }
@@ -405,10 +405,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
         for (int g = 0; g < G && ok; ++g, ++gg) {
           const uint32_t dbuf = tmem + (uint32_t)((gg & 1) * kBufCols);
           for (int c = 0; c < kg; ++c, ++q) {
+            // polling with a short back-off: spinning threads take issue slots
+            // from the converter and epilogue warps
             for (int i = 0; i < kMaxWait && avail <= (uint32_t)q; ++i) {
               asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(avail)
                            : "r"(su32(&ready)) : "memory");
-              if (*abrt) break;
+              if (avail > (uint32_t)q || *abrt) break;
+              __nanosleep(16);
             }
             if (avail <= (uint32_t)q) { ok = false; *abrt = 1; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
