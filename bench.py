@@ -19,9 +19,9 @@ path, K iterations after W warm-up iterations.  time_to_scf: complete runs
 from the superposition guess to |dE| < 1e-5 Ha/atom with the mixed and the
 FP64 filters (and the learned initial guess when a trained model is present).
 
---impl reference times the FP64 CPU restatement of the same iteration (the
-reference's algorithm; the reference itself cannot be built here) on all host
-cores, on a bounded sample scaled to one iteration.
+--impl reference times one complete FP64 SCF iteration of the same workload by
+the CPU restatement of the reference's algorithm (the reference itself cannot
+be built here) on all host cores.
 
 N > 1 runs independent replicas (the path has no data-path exchange at one
 block per GPU); value = max-over-ranks time per iteration.
@@ -394,29 +394,41 @@ def cpu_baseline(s, passes, rho_host, g, scale=True):
 
 
 def run_reference(args, rank, world):
+    """The reference's algorithm on the host cores: one complete FP64 SCF
+    iteration of the same workload by the CPU restatement (oracle/scf.py:
+    Tucker decompositions, 35-term Hartree, LDA, H values on the pattern,
+    Lanczos, the GPU arm's steady-state number of Chebyshev passes with
+    Cholesky-QR and Rayleigh-Ritz, Fermi level, density, energy), timed as
+    it runs.  One iteration takes minutes on the host, so --steps and
+    --warmup are not repeated: the line reports steps 1, warmup 0."""
     if rank != 0:
         return
-    s = make_system()
-    from ttdft_public_gb300 import scf as _scf  # noqa: F401  (system model only)
+    from oracle import scf as oscf
     import oracle
+    s = make_system()
+    passes = 2
+    cfg = scf_config("fp64", restarts_first=passes, restarts_other=passes)
+    t0 = time.perf_counter()
+    o = oscf.OracleScf(s, cfg)
+    setup_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    o.run(max_iter=1)
+    v = time.perf_counter() - t0
     q = [b.fem.nq for b in s.basis]
-    rho = oracle.sad_density(s.atoms, [b.fem.xq for b in s.basis], s.spec.z_val, 1.0)
-    vals = []
-    c = None
-    for i in range(args.warmup + args.steps):
-        c = cpu_baseline(s, 2.0, rho.reshape(-1), None)
-        if i >= args.warmup:
-            vals.append(c["value"])
-    v = float(np.mean(vals))
-    c["value"] = v
+    sample = (f"one complete FP64 SCF iteration of {WORKLOAD} by the CPU restatement of the "
+              f"reference's algorithm ({passes} Chebyshev passes of degree {s.spec.degree}, the "
+              f"GPU arm's steady state; Tucker decompositions, Hartree, LDA, H values, density, "
+              f"energy), measured, not scaled; set-up {setup_s:.0f} s not counted")
+    c = {"value": v, "unit": "s/SCF-iter", "cores": oracle.threads(), "kind": "port",
+         "sample": sample}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s/SCF-iter",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
+            "n_gpus": world, "steps": 1, "warmup": 0, "ms_per_step": v * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
             "data": "synthetic (seeded atoms)",
-            "config": {"workload": f"{WORKLOAD}: full SCF iteration (CPU sample, 2 filter "
-                                   f"passes per iteration)", "N": s.N,
-                       "states": s.spec.n_states, "degree": s.spec.degree,
-                       "quad_points": int(np.prod(q))},
+            "config": {"workload": f"{WORKLOAD}: full SCF iteration (FP64, host cores)",
+                       "N": s.N, "states": s.spec.n_states, "degree": s.spec.degree,
+                       "quad_points": int(np.prod(q)), "passes_per_iter": passes,
+                       "steps_requested": args.steps, "warmup_requested": args.warmup},
             "cpu_baseline": c,
             "e2e": {"value": v, "unit": "s/SCF-iter", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
