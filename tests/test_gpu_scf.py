@@ -194,3 +194,26 @@ def test_tucker_files_restart_the_scf(tmp_path):
         assert abs(res2["energy"] - res["energy"]) / spec.n_atoms < 1e-5
     finally:
         g2.close()
+
+
+def test_restart_tree_resumes_the_scf(scf_system, tmp_path):
+    """An SCF stopped after four iterations and resumed from its restart tree
+    (eigenvectors, Chebyshev bounds, Anderson history; main.cc:754-802,
+    dft/AndersonMixing.cc:84-143) continues exactly as the uninterrupted run."""
+    base = {**cfg().__dict__, "filter": "fp64"}
+    full = scf.Scf(scf_system, scf.ScfConfig(**base)).run()
+    g1 = scf.Scf(scf_system, scf.ScfConfig(**{**base, "max_iter": 4, "restart_dir": str(tmp_path)}))
+    try:
+        g1.run()
+    finally:
+        g1.close()
+    g2 = scf.Scf(scf_system, scf.ScfConfig(**{**base, "restart_dir": str(tmp_path), "resume": True}))
+    try:
+        res = g2.run()
+    finally:
+        g2.close()
+    assert res["history"][0]["iter"] == 4
+    e_full = np.array([h["energy"] for h in full["history"]])
+    e_res = np.array([h["energy"] for h in res["history"]])
+    assert len(e_res) == len(e_full) - 4
+    assert np.abs(e_res - e_full[4:]).max() < 1e-9

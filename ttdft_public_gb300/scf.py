@@ -32,7 +32,7 @@ import time
 
 import numpy as np
 
-from . import _lib, api, tucker_io
+from . import _lib, api, restart, tucker_io
 from ._lib import check
 from .kernel_expansion import coulomb_expansion
 
@@ -74,6 +74,11 @@ class ScfConfig:
     # tucker_input_factor_{x,y,z} (InitialGuess::initialize_rho_tucker)
     tucker_dir: str = ""
     seed: int = 0
+    # restart tree (restart.py; main.cc:690-802, 1146-1173): written after
+    # every iteration when restart_dir is set; resume=True continues the run
+    # recorded there (X, the Chebyshev bounds, the Anderson history)
+    restart_dir: str = ""
+    resume: bool = False
 
 
 def cheb_schedule(cfg: ScfConfig, m: int):
@@ -351,11 +356,29 @@ class Scf:
         lower_wanted = lower_unwanted = None
         occ_energy = 1e9
         e_old = None
-        rho_in = self.initial_density() if rho0 is None else rho0
+        ranks = [bb.r for bb in self.s.basis]
+        start = 0
+        if cfg.resume:
+            # the state a previous run left after its last iteration
+            b = restart.read_bounds(cfg.restart_dir, ranks)
+            X.set(restart.read_wfn(cfg.restart_dir, ranks, self.s.N, k))
+            upper, err_upper = b["upper"], b["err_upper"]
+            lower_wanted, lower_unwanted = b["lower_wanted"], b["lower_unwanted"]
+            occ_energy, e_old = b["occ_energy"], b["e_old"]
+            kept = restart.read_history(cfg.restart_dir, ranks)
+            for i in kept:
+                hist_in.append(self._dev(restart.read_array(
+                    restart.rho_file(cfg.restart_dir, ranks, "quad_in", i), self.nq)))
+                hist_out.append(self._dev(restart.read_array(
+                    restart.rho_file(cfg.restart_dir, ranks, "quad_out", i), self.nq)))
+            start = kept[-1] + 1 if kept else 0
+            rho_in = hist_in[-1] if hist_in else self.initial_density()
+        else:
+            rho_in = self.initial_density() if rho0 is None else rho0
         self.rho_start = rho_in
         sch = cheb_schedule(cfg, m)
         w = None
-        for it in range(max_iter):
+        for it in range(start, max_iter):
             t_it = time.perf_counter()
             ph = {}
             mark = [t_it]
@@ -388,7 +411,7 @@ class Scf:
                 if it == 0:
                     lower_wanted, lower_unwanted = tmp_lower, 0.0
             lap("lanczos")
-            if it > 0:
+            if it > 0 and w is not None:
                 lower_wanted, lower_unwanted = w[0], w[-1]
             restarts = cfg.restarts_first if it == 0 else cfg.restarts_other
             n_pass = 0
@@ -441,6 +464,15 @@ class Scf:
             self.eigenvalues, self.X, self.rho = w, X, rho_out
             self.upper_bound = upper
             e_old = energy
+            if cfg.restart_dir:
+                restart.write_bounds(cfg.restart_dir, ranks, {
+                    "upper": upper, "lower_unwanted": w[-1], "lower_wanted": w[0],
+                    "err_upper": err_upper, "occ_energy": occ_energy, "e_old": energy})
+                restart.write_wfn(cfg.restart_dir, ranks, X.get())
+                restart.write_history_entry(
+                    cfg.restart_dir, ranks, it,
+                    {"quad_in": rho_in.cpu().numpy(), "quad_out": rho_out.cpu().numpy(),
+                     "nodal_out": self.rho_nodal.cpu().numpy()}, cfg.history)
             yield rec
             if de is not None and de < tol and drho2 < cfg.tol_drho2:
                 break
