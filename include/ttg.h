@@ -256,6 +256,11 @@ ttg_status ttg_op_set_kinetic(ttg_op* op, const double* dx, const double* dy, co
  * Entries the pattern does not hold are not created. */
 ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const double* G,
                                    const double* px, const double* py, const double* pz);
+/* ttg_op_update_potential with G and the potential matrices in device memory,
+ * on the op's stream, without synchronising. */
+ttg_status ttg_op_update_potential_device(ttg_op* op, const int32_t* pot_ranks,
+                                          const double* g_dev, const double* px_dev,
+                                          const double* py_dev, const double* pz_dev);
 
 /* ---- SCF grid kernels (FP64, device pointers, x-fastest fields) ------------ */
 

@@ -102,6 +102,7 @@ _SIGS = {
     "ttg_hartree_device": [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                            c_vp, c_vp],
     "ttg_density_device": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32],
+    "ttg_op_update_potential_device": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
     "ttg_tc_gemm": [c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_i32, c_vp, c_i64, c_vp],
     "ttg_atom_descriptors": [c_i32, c_vp, c_i32, c_dbl, c_dbl, c_dbl, c_dbl, c_vp],
     "ttg_mlp_create": [c_i32, c_vp, c_vp],

@@ -130,69 +130,61 @@ __global__ void k_update_values(UpdateArgs a) {
 
 using namespace ttg;
 
-extern "C" {
+namespace ttg {
+namespace {
 
-ttg_status ttg_op_set_kinetic(ttg_op* op, const double* dx, const double* dy, const double* dz,
-                              const double* mx, const double* my, const double* mz) {
-  if (!op || !op->keep_pattern || !dx || !dy || !dz || !mx || !my || !mz) return TTG_BAD_ARG;
+// pair tables PXp[xp][a] = PX_a[i][j], xp = i (2b + 1) + (j - i) + b, from
+// the (rk x r x r) row-major matrices on the device
+__global__ void k_pair_table(const double* __restrict__ pm, int r, int rk, int b,
+                             double* __restrict__ out) {
+  const int64_t np = (int64_t)r * (2 * b + 1);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < np * rk;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = e / rk;
+    const int a = (int)(e - p * rk);
+    const int i = (int)(p / (2 * b + 1));
+    const int j = i + (int)(p - (int64_t)i * (2 * b + 1)) - b;
+    out[e] = (j >= 0 && j < r) ? pm[((int64_t)a * r + i) * r + j] : 0.0;
+  }
+}
+
+struct UpdateLayout {
+  int ra, rb, rc;
+  int64_t nxp, nyp, nzp, off_x, off_y, off_z, off_g, off_t1, off_t2, total;
+};
+
+ttg_status update_layout(ttg_op* op, const int32_t* pot_ranks, UpdateLayout& L) {
   Pattern& P = op->pattern;
-  const int rx = P.r[0], ry = P.r[1], rz = P.r[2];
-  const size_t cnt = 2 * ((size_t)rx * rx + (size_t)ry * ry + (size_t)rz * rz);
-  if (!P.kin.p) TTG_TRY(P.kin.alloc(cnt * 8));
-  std::vector<double> h;
-  h.reserve(cnt);
-  h.insert(h.end(), dx, dx + rx * rx);
-  h.insert(h.end(), dy, dy + ry * ry);
-  h.insert(h.end(), dz, dz + rz * rz);
-  h.insert(h.end(), mx, mx + rx * rx);
-  h.insert(h.end(), my, my + ry * ry);
-  h.insert(h.end(), mz, mz + rz * rz);
-  TTG_CUDA_TRY(cudaMemcpyAsync(P.kin.p, h.data(), cnt * 8, cudaMemcpyHostToDevice, op->stream));
-  TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
-  P.kinetic_set = true;
+  L.ra = pot_ranks[0];
+  L.rb = pot_ranks[1];
+  L.rc = pot_ranks[2];
+  if (L.ra <= 0 || L.rb <= 0 || L.rc <= 0) return TTG_BAD_ARG;
+  L.nxp = (int64_t)P.r[0] * (2 * P.bw[0] + 1);
+  L.nyp = (int64_t)P.r[1] * (2 * P.bw[1] + 1);
+  L.nzp = (int64_t)P.r[2] * (2 * P.bw[2] + 1);
+  const int64_t ncore = (int64_t)L.ra * L.rb * L.rc;
+  L.off_x = 0;
+  L.off_y = L.off_x + L.nxp * L.ra;
+  L.off_z = L.off_y + L.nyp * L.rb;
+  L.off_g = L.off_z + L.nzp * L.rc;
+  L.off_t1 = L.off_g + ncore;
+  L.off_t2 = L.off_t1 + L.nxp * L.rb * L.rc;
+  L.total = L.off_t2 + L.nyp * L.nxp * L.rc;
+  if ((int64_t)P.work.bytes < L.total * 8) TTG_TRY(P.work.alloc(L.total * 8));
   return TTG_OK;
 }
 
-ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const double* G,
-                                   const double* px, const double* py, const double* pz) {
-  if (!op || !op->keep_pattern || !op->pattern.kinetic_set || !pot_ranks || !G || !px || !py ||
-      !pz)
-    return TTG_BAD_ARG;
+// T1, T2 and the per-entry update, from the pair tables and the core in work
+ttg_status update_from_tables(ttg_op* op, const UpdateLayout& L) {
   Pattern& P = op->pattern;
   const int rx = P.r[0], ry = P.r[1], rz = P.r[2];
-  const int ra = pot_ranks[0], rb = pot_ranks[1], rc = pot_ranks[2];
-  if (ra <= 0 || rb <= 0 || rc <= 0) return TTG_BAD_ARG;
+  const int ra = L.ra, rb = L.rb, rc = L.rc;
   const int bw[3] = {P.bw[0], P.bw[1], P.bw[2]};
-  const int64_t nxp = (int64_t)rx * (2 * bw[0] + 1);
-  const int64_t nyp = (int64_t)ry * (2 * bw[1] + 1);
-  const int64_t nzp = (int64_t)rz * (2 * bw[2] + 1);
-  // pair tables PXp[xp][a] = PX_a[i][j] (host: O(pairs * rank))
-  auto pairs = [](const double* pm, int r, int rk, int b, std::vector<double>& out) {
-    const int64_t np = (int64_t)r * (2 * b + 1);
-    out.assign(np * rk, 0.0);
-    for (int i = 0; i < r; ++i)
-      for (int d = -b; d <= b; ++d) {
-        const int j = i + d;
-        if (j < 0 || j >= r) continue;
-        const int64_t p = (int64_t)i * (2 * b + 1) + d + b;
-        for (int a = 0; a < rk; ++a) out[p * rk + a] = pm[((int64_t)a * r + i) * r + j];
-      }
-  };
-  std::vector<double> hx, hy, hz;
-  pairs(px, rx, ra, bw[0], hx);
-  pairs(py, ry, rb, bw[1], hy);
-  pairs(pz, rz, rc, bw[2], hz);
-  const int64_t ncore = (int64_t)ra * rb * rc;
-  const int64_t off_x = 0, off_y = off_x + nxp * ra, off_z = off_y + nyp * rb;
-  const int64_t off_g = off_z + nzp * rc, off_t1 = off_g + ncore;
-  const int64_t off_t2 = off_t1 + nxp * rb * rc, total = off_t2 + nyp * nxp * rc;
-  if ((int64_t)P.work.bytes < total * 8) TTG_TRY(P.work.alloc(total * 8));
+  const int64_t nxp = L.nxp, nyp = L.nyp;
+  const int64_t off_x = L.off_x, off_y = L.off_y, off_z = L.off_z, off_g = L.off_g,
+                off_t1 = L.off_t1, off_t2 = L.off_t2;
   double* w = P.work.as<double>();
   cudaStream_t st = op->stream;
-  TTG_CUDA_TRY(cudaMemcpyAsync(w + off_x, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice, st));
-  TTG_CUDA_TRY(cudaMemcpyAsync(w + off_y, hy.data(), hy.size() * 8, cudaMemcpyHostToDevice, st));
-  TTG_CUDA_TRY(cudaMemcpyAsync(w + off_z, hz.data(), hz.size() * 8, cudaMemcpyHostToDevice, st));
-  TTG_CUDA_TRY(cudaMemcpyAsync(w + off_g, G, ncore * 8, cudaMemcpyHostToDevice, st));
   // T1[b][xp][c] = sum_a PXp[xp][a] G[a + ra (b + rb c)]   (batch over b)
   TTG_TRY(dgemm(st, (int)nxp, rc, ra, rb, DOp{w + off_x, ra, 1, 0},
                 DOp{w + off_g, 1, (int64_t)ra * rb, ra}, w + off_t1, rc, 1, nxp * rc, P.work2));
@@ -226,8 +218,96 @@ ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const d
   const int wpb = 8;
   k_update_values<<<(unsigned)((op->n + wpb - 1) / wpb), 32 * wpb, 0, st>>>(a); TTG_COUNT();
   TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+}  // namespace
+}  // namespace ttg
+
+
+extern "C" {
+
+ttg_status ttg_op_set_kinetic(ttg_op* op, const double* dx, const double* dy, const double* dz,
+                              const double* mx, const double* my, const double* mz) {
+  if (!op || !op->keep_pattern || !dx || !dy || !dz || !mx || !my || !mz) return TTG_BAD_ARG;
+  Pattern& P = op->pattern;
+  const int rx = P.r[0], ry = P.r[1], rz = P.r[2];
+  const size_t cnt = 2 * ((size_t)rx * rx + (size_t)ry * ry + (size_t)rz * rz);
+  if (!P.kin.p) TTG_TRY(P.kin.alloc(cnt * 8));
+  std::vector<double> h;
+  h.reserve(cnt);
+  h.insert(h.end(), dx, dx + rx * rx);
+  h.insert(h.end(), dy, dy + ry * ry);
+  h.insert(h.end(), dz, dz + rz * rz);
+  h.insert(h.end(), mx, mx + rx * rx);
+  h.insert(h.end(), my, my + ry * ry);
+  h.insert(h.end(), mz, mz + rz * rz);
+  TTG_CUDA_TRY(cudaMemcpyAsync(P.kin.p, h.data(), cnt * 8, cudaMemcpyHostToDevice, op->stream));
+  TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
+  P.kinetic_set = true;
+  return TTG_OK;
+}
+
+ttg_status ttg_op_update_potential(ttg_op* op, const int32_t* pot_ranks, const double* G,
+                                   const double* px, const double* py, const double* pz) {
+  if (!op || !op->keep_pattern || !op->pattern.kinetic_set || !pot_ranks || !G || !px || !py ||
+      !pz)
+    return TTG_BAD_ARG;
+  Pattern& P = op->pattern;
+  UpdateLayout L;
+  TTG_TRY(update_layout(op, pot_ranks, L));
+  // pair tables PXp[xp][a] = PX_a[i][j] (host: O(pairs * rank))
+  auto pairs = [](const double* pm, int r, int rk, int b, std::vector<double>& out) {
+    const int64_t np = (int64_t)r * (2 * b + 1);
+    out.assign(np * rk, 0.0);
+    for (int i = 0; i < r; ++i)
+      for (int d = -b; d <= b; ++d) {
+        const int j = i + d;
+        if (j < 0 || j >= r) continue;
+        const int64_t p = (int64_t)i * (2 * b + 1) + d + b;
+        for (int a = 0; a < rk; ++a) out[p * rk + a] = pm[((int64_t)a * r + i) * r + j];
+      }
+  };
+  std::vector<double> hx, hy, hz;
+  pairs(px, P.r[0], L.ra, P.bw[0], hx);
+  pairs(py, P.r[1], L.rb, P.bw[1], hy);
+  pairs(pz, P.r[2], L.rc, P.bw[2], hz);
+  double* w = P.work.as<double>();
+  cudaStream_t st = op->stream;
+  const int64_t ncore = (int64_t)L.ra * L.rb * L.rc;
+  TTG_CUDA_TRY(cudaMemcpyAsync(w + L.off_x, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice, st));
+  TTG_CUDA_TRY(cudaMemcpyAsync(w + L.off_y, hy.data(), hy.size() * 8, cudaMemcpyHostToDevice, st));
+  TTG_CUDA_TRY(cudaMemcpyAsync(w + L.off_z, hz.data(), hz.size() * 8, cudaMemcpyHostToDevice, st));
+  TTG_CUDA_TRY(cudaMemcpyAsync(w + L.off_g, G, ncore * 8, cudaMemcpyHostToDevice, st));
+  TTG_TRY(update_from_tables(op, L));
   TTG_CUDA_TRY(cudaStreamSynchronize(st));
   return TTG_OK;
+}
+
+ttg_status ttg_op_update_potential_device(ttg_op* op, const int32_t* pot_ranks,
+                                          const double* g_dev, const double* px_dev,
+                                          const double* py_dev, const double* pz_dev) {
+  if (!op || !op->keep_pattern || !op->pattern.kinetic_set || !pot_ranks || !g_dev || !px_dev ||
+      !py_dev || !pz_dev)
+    return TTG_BAD_ARG;
+  Pattern& P = op->pattern;
+  UpdateLayout L;
+  TTG_TRY(update_layout(op, pot_ranks, L));
+  double* w = P.work.as<double>();
+  cudaStream_t st = op->stream;
+  const double* pm[3] = {px_dev, py_dev, pz_dev};
+  const int rk[3] = {L.ra, L.rb, L.rc};
+  const int64_t off[3] = {L.off_x, L.off_y, L.off_z};
+  const int64_t np[3] = {L.nxp, L.nyp, L.nzp};
+  for (int d = 0; d < 3; ++d) {
+    const int64_t n = np[d] * rk[d];
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    k_pair_table<<<std::max(blocks, 1), 256, 0, st>>>(pm[d], P.r[d], rk[d], P.bw[d], w + off[d]); TTG_COUNT();
+    TTG_LAUNCHED(op);
+  }
+  TTG_CUDA_TRY(cudaMemcpyAsync(w + L.off_g, g_dev, (size_t)L.ra * L.rb * L.rc * 8,
+                               cudaMemcpyDeviceToDevice, st));
+  return update_from_tables(op, L);
 }
 
 }  // extern "C"

@@ -148,6 +148,12 @@ class Scf:
         self.alpha_dev, self.omega_dev = self._dev(self.alpha), self._dev(self.omega)
         # basis values at the nodes (n_d x r_d column-major) for the density
         self.unodal_dev = [self._dev(np.asfortranarray(bb.nodal).reshape(-1, order="F")) for bb in b]
+        # nodes -> quadrature points (q_d x n_d) and the products of basis
+        # functions at the quadrature points, weighted (q_d x r_d^2): the
+        # potential matrices of a factor U are then one GEMM, U^T M
+        self.interp_dev = [self._dev(bb.fem.interp_matrix()) for bb in b]
+        self.pmat_dev = [self._dev(((bb.quad * bb.fem.wJ[:, None])[:, :, None]
+                                    * bb.quad[:, None, :]).reshape(bb.fem.nq, -1)) for bb in b]
         # fixed local potential: Gaussian wells + neutralising ionic charges
         self.vloc = self._zeros()
         fx = [np.stack([np.exp(-(self.xq[d] - a[d]) ** 2 / (2 * spec.sigma ** 2)) for a in sysm.atoms])
@@ -210,9 +216,11 @@ class Scf:
                                         1 if take_abs else 0, self.st), "ttg_grid_lincomb")
         return out
 
-    def sthosvd(self, field, dims, eps, cap):
-        """Tucker decomposition on the device; returns (core, [U_d]) on host.
-        cap: one rank cap for all directions, or one per direction."""
+    def sthosvd(self, field, dims, eps, cap, device=False):
+        """Tucker decomposition on the device; returns (core, [U_d], ranks),
+        on the host, or with device=True as device tensors: the core flat and
+        x fastest, each U_d flat n_d x r_d column-major.  cap: one rank cap for
+        all directions, or one per direction."""
         torch = self.torch
         cap3 = list(cap) if np.ndim(cap) else [cap] * 3
         caps = np.array([min(int(c), int(d)) for c, d in zip(cap3, dims)], np.int32)
@@ -224,6 +232,8 @@ class Scf:
                                           float(eps), _lib.ptr(caps), _lib.ptr(ranks), self._p(core),
                                           *[self._p(u) for u in U]), "ttg_tucker_sthosvd")
         r = [int(x) for x in ranks]
+        if device:
+            return core[: r[0] * r[1] * r[2]], [U[d][: int(dims[d]) * r[d]] for d in range(3)], r
         G = core[: r[0] * r[1] * r[2]].cpu().numpy()
         Uh = [U[d][: int(dims[d]) * r[d]].cpu().numpy().reshape(r[d], int(dims[d])).T.copy()
               for d in range(3)]
@@ -233,8 +243,7 @@ class Scf:
         """V_H on the quadrature grid (device, FP64) from a Tucker density with
         factors at the quad points: ttg_hartree_device on the operator's
         stream, all expansion terms in one tensor-core contraction."""
-        core = self._dev(np.ascontiguousarray(G).reshape(-1))
-        U = [self._dev(np.asfortranarray(Uq[d]).reshape(-1, order="F")) for d in range(3)]
+        core, U = self._tucker_dev(G, Uq)
         V = self._zeros()
         vp = lambda ts: (ctypes.c_void_p * 3)(*[t.data_ptr() for t in ts])  # noqa: E731
         check(self.lib.ttg_hartree_device(self.op.h, self.alpha.size, self._p(self.alpha_dev),
@@ -244,7 +253,18 @@ class Scf:
                                           self._p(V)), "ttg_hartree_device")
         return V
 
+    def _tucker_dev(self, G, U):
+        """(core, factors) as device tensors: the core flat and x fastest,
+        factors flat column-major; host arrays (factors n x r) are uploaded."""
+        if isinstance(G, self.torch.Tensor):
+            return G, U
+        return (self._dev(np.ascontiguousarray(G).reshape(-1)),
+                [self._dev(np.asfortranarray(u).reshape(-1, order="F")) for u in U])
+
     def hartree_energy(self, G, Uq, r):
+        if isinstance(G, self.torch.Tensor):
+            G = G.cpu().numpy()
+            Uq = [u.cpu().numpy().reshape(r[d], -1).T for d, u in enumerate(Uq)]
         quad = [(self.xq[d], self.fem_w(d)) for d in range(3)]
         return api.hartree_energy(self.alpha, self.omega, G.reshape(r[2], r[1], r[0]), quad, Uq)
 
@@ -253,8 +273,7 @@ class Scf:
 
     def reconstruct(self, G, U, r, dims):
         torch = self.torch
-        core = self._dev(G)
-        Ud = [self._dev(np.asfortranarray(U[d]).reshape(-1, order="F")) for d in range(3)]
+        core, Ud = self._tucker_dev(G, U)
         out = torch.zeros(int(np.prod(dims)), dtype=torch.float64, device=self.dev)
         check(self.lib.ttg_tucker_reconstruct(self._p(core), _lib.ptr(np.array(r, np.int32)),
                                               *[self._p(u) for u in Ud],
@@ -297,7 +316,7 @@ class Scf:
     def veff_from(self, rho_in):
         """V_eff = V_loc + V_H(rho_in) + V_xc(rho_in) on the quad grid."""
         cfg = self.cfg
-        G, U, r = self.sthosvd(rho_in, self.qdims, cfg.rho_eps, cfg.rho_rank_cap)
+        G, U, r = self.sthosvd(rho_in, self.qdims, cfg.rho_eps, cfg.rho_rank_cap, device=True)
         vh = self.hartree(G, U, r)
         veff = self.lincomb([vh, self.vloc], [1.0, 1.0], vh)
         check(self.lib.ttg_grid_lda(self._p(rho_in), self.nq, self._p(veff), None, 1, self.st),
@@ -305,11 +324,15 @@ class Scf:
         return veff
 
     def update_hamiltonian(self, veff):
-        G, U, r = self.sthosvd(veff, self.qdims, self.cfg.veff_eps, self.cfg.veff_rank_cap)
-        P = [potential_matrices(self.s.basis[d], U[d]) for d in range(3)]
-        check(self.lib.ttg_op_update_potential(self.op.h, _lib.ptr(np.array(r, np.int32)),
-                                               _lib.ptr(np.ascontiguousarray(G)),
-                                               *[_lib.ptr(p) for p in P]), "ttg_op_update_potential")
+        """Tucker decomposition of V_eff and the new H values, all on the
+        device: the potential matrices PX_a = U^T M (potential_matrices) as
+        one GEMM per direction."""
+        G, U, r = self.sthosvd(veff, self.qdims, self.cfg.veff_eps, self.cfg.veff_rank_cap,
+                               device=True)
+        P = [(U[d].view(r[d], self.q[d]) @ self.pmat_dev[d]).contiguous() for d in range(3)]
+        check(self.lib.ttg_op_update_potential_device(self.op.h, _lib.ptr(np.array(r, np.int32)),
+                                                      self._p(G), *[self._p(p) for p in P]),
+              "ttg_op_update_potential_device")
         self.veff_ranks = r
 
     def density_out(self, X, occ):
@@ -323,8 +346,11 @@ class Scf:
                                           _lib.ptr(self.ndims), *[self._p(u) for u in self.unodal_dev],
                                           self._p(rho_nd), 0), "ttg_density_device")
         self.rho_nodal = rho_nd
-        G, U, r = self.sthosvd(rho_nd, self.ndims, self.cfg.rho_out_eps, self.cfg.rho_out_rank_cap)
-        Uq = [self.s.basis[d].fem.interp_matrix() @ U[d] for d in range(3)]
+        G, U, r = self.sthosvd(rho_nd, self.ndims, self.cfg.rho_out_eps, self.cfg.rho_out_rank_cap,
+                               device=True)
+        # factors at the quadrature points, column-major q_d x r_d
+        Uq = [(self.interp_dev[d] @ U[d].view(r[d], int(self.ndims[d])).T).T.contiguous().view(-1)
+              for d in range(3)]
         raw = self.reconstruct(G, Uq, r, self.qdims)
         rho = self.lincomb([raw], [1.0], self._zeros(), take_abs=True)
         return rho, (G, Uq, r, raw)
