@@ -1,6 +1,7 @@
 """The tcgen05 (tensor-memory) FP32 filter degree against the FP64 oracle and
 against the mma.sync tensor-core kernel.  The kernel runs for block widths
-that are multiples of 16 up to 256.  Its three-term BF16 split keeps FP32
+that are multiples of 16 up to 256, wider blocks (288 here) in column blocks
+of at most 256.  Its three-term BF16 split keeps FP32
 accuracy, so the FP32 bound of the other FP32 kernels (5e-5 of the block's
 largest entry after a 10-degree filter) applies; the kernel's own error is
 reported by the tests as well."""
@@ -33,7 +34,7 @@ def bounds(s, v_seed=6):
     return 0.0, up, lo
 
 
-@pytest.mark.parametrize("k", [16, 48, 160])
+@pytest.mark.parametrize("k", [16, 48, 160, 288])
 @pytest.mark.parametrize("tucker", [True, False])
 def test_umma_filter_matches_oracle(small_system, k, tucker):
     s = small_system
@@ -124,3 +125,20 @@ def test_umma_filter_after_potential_update():
         assert rel(Y, ref) < 5e-5
     finally:
         g.close()
+
+
+def test_umma_bf16_degree_in_column_blocks(small_system):
+    """A 288-wide block takes two tcgen05 launches per BF16 degree (144 + 144
+    columns); each column's result is the one a narrow block gives."""
+    s = small_system
+    op = api.Operator(api.ProjectHamiltonianSparse.from_system(s), 288)
+    try:
+        a, b, a0 = bounds(s)
+        X = np.random.default_rng(77).standard_normal((s.N, 288))
+        Y = run_filter(op, s, X, 1, a, b, a0, prec="bf16")
+        Y48 = run_filter(op, s, X[:, 144:192], 1, a, b, a0, prec="bf16")
+        assert np.array_equal(Y[:, 144:192], Y48)
+        ref = oracle.cheb_filter(s, X, 1, a, b, a0)
+        assert rel(Y, ref) < 2e-2
+    finally:
+        op.close()

@@ -699,6 +699,21 @@ ttg_status launch_cheb_step(ttg_op* op, int prec, const void* src, const void* x
   if (k <= 0 || k > op->max_k) return TTG_BAD_ARG;
   if (umma_supported(op, prec, k))
     return launch_cheb_umma(op, prec, src, xold, dst, k, alpha, beta, delta);
+  // blocks wider than one MMA (N <= 256): the tcgen05 degree over column
+  // blocks of at most 256 states, each re-reading H (the reference's
+  // num_X_blocks, ChebyShevFilter.cc:97-170, splits its columns the same way)
+  if (k > 256 && k % 16 == 0 && umma_supported(op, prec, 256)) {
+    const int nblk = (k + 255) / 256;
+    const int kb = ((k + nblk - 1) / nblk + 15) / 16 * 16;
+    const size_t elem = prec == TTG_PREC_FP32 ? 4 : 2;
+    for (int c0 = 0; c0 < k; c0 += kb) {
+      const int kk = std::min(kb, k - c0);
+      TTG_TRY(launch_cheb_umma(op, prec, static_cast<const char*>(src) + c0 * elem,
+                               xold ? static_cast<const char*>(xold) + c0 * elem : nullptr,
+                               static_cast<char*>(dst) + c0 * elem, kk, alpha, beta, delta));
+    }
+    return TTG_OK;
+  }
   if (tc_supported(op, prec, k))
     return launch_cheb_tc(op, prec, src, xold, dst, k, alpha, beta, delta);
   if (prec == TTG_PREC_FP64) {
