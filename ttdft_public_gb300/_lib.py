@@ -36,8 +36,11 @@ def host():
             from . import build
             build.build_host()
         _host = ctypes.CDLL(path)
-        for name in ("ttg_host_assemble_hloc", "ttg_host_assemble_cnloc"):
+        for name in ("ttg_host_assemble_hloc", "ttg_host_assemble_cnloc",
+                     "ttg_host_assemble_hloc_once"):
             getattr(_host, name).restype = ctypes.c_int
+        _host.ttg_host_free.restype = None
+        _host.ttg_host_free.argtypes = [ctypes.c_void_p]
     return _host
 
 

@@ -21,6 +21,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <cstdlib>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -55,6 +56,92 @@ Sparse1D make_sparse(const double* m, int r, double drop) {
   }
   return s;
 }
+
+// Scratch of one thread: a dense row accumulator and the list of touched columns.
+struct RowScratch {
+  std::vector<double> row;
+  std::vector<char> touched;
+  std::vector<int> touched_list;
+  explicit RowScratch(int64_t n) : row(n, 0.0), touched(n, 0) { touched_list.reserve(1 << 16); }
+};
+
+// Builds one row of H_loc: the kinetic and potential Kronecker sums, then
+// the entries above the truncation in column order.
+struct RowBuilder {
+  int rx, ry, rz;
+  int64_t N;
+  const Sparse1D *sMX, *sMY, *sMZ, *sDX, *sDY, *sDZ;
+  const std::vector<Sparse1D>*sPX, *sPY, *sPZ;
+  int nterm;
+  const double* coef;
+  double truncation, prune;
+
+  void row(int64_t I, RowScratch& s, std::vector<int>& out_cols,
+           std::vector<double>& out_vals) const {
+    std::vector<double>& row = s.row;
+    std::vector<char>& touched = s.touched;
+    std::vector<int>& touched_list = s.touched_list;
+    auto add = [&](int64_t J, double v) {
+      if (!touched[J]) {
+        touched[J] = 1;
+        touched_list.push_back((int)J);
+      }
+      row[J] += v;
+    };
+      const int xI = (int)(I % rx);
+      const int yI = (int)((I / rx) % ry);
+      const int zI = (int)(I / ((int64_t)rx * ry));
+      // kinetic: 0.5*(DX MY MZ + MX DY MZ + MX MY DZ)
+      const Sparse1D* A[3][3] = {{sDX, sMY, sMZ}, {sMX, sDY, sMZ}, {sMX, sMY, sDZ}};
+      for (int term = 0; term < 3; ++term) {
+        const Sparse1D &ax = *A[term][0], &ay = *A[term][1], &az = *A[term][2];
+        for (int64_t pz = az.ptr[zI]; pz < az.ptr[zI + 1]; ++pz) {
+          const int zJ = az.col[pz];
+          const double vz = 0.5 * az.val[pz];
+          // products that cannot reach the truncation are not formed
+          if (std::fabs(vz) * ay.rowmax[yI] * ax.rowmax[xI] <= prune) continue;
+          for (int64_t py = ay.ptr[yI]; py < ay.ptr[yI + 1]; ++py) {
+            const int yJ = ay.col[py];
+            const double vyz = vz * ay.val[py];
+            if (std::fabs(vyz) * ax.rowmax[xI] <= prune) continue;
+            const int64_t base = (int64_t)rx * (yJ + (int64_t)ry * zJ);
+            for (int64_t px = ax.ptr[xI]; px < ax.ptr[xI + 1]; ++px)
+              add(base + ax.col[px], vyz * ax.val[px]);
+          }
+        }
+      }
+      // potential: sum_t coef_t PX_t PY_t PZ_t
+      for (int t = 0; t < nterm; ++t) {
+        const Sparse1D &px = (*sPX)[t], &py = (*sPY)[t], &pz = (*sPZ)[t];
+        const double bound = std::fabs(coef[t]) * px.rowmax[xI] * py.rowmax[yI] * pz.rowmax[zI];
+        if (bound <= prune) continue;
+        for (int64_t qz = pz.ptr[zI]; qz < pz.ptr[zI + 1]; ++qz) {
+          const int zJ = pz.col[qz];
+          const double wz = coef[t] * pz.val[qz];
+          if (std::fabs(wz) * py.rowmax[yI] * px.rowmax[xI] <= prune) continue;
+          for (int64_t qy = py.ptr[yI]; qy < py.ptr[yI + 1]; ++qy) {
+            const int yJ = py.col[qy];
+            const double w = wz * py.val[qy];
+            if (std::fabs(w) * px.rowmax[xI] <= prune) continue;
+            const int64_t base = (int64_t)rx * (yJ + (int64_t)ry * zJ);
+            for (int64_t qx = px.ptr[xI]; qx < px.ptr[xI + 1]; ++qx)
+              add(base + px.col[qx], w * px.val[qx]);
+          }
+        }
+      }
+      std::sort(touched_list.begin(), touched_list.end());
+      for (int J : touched_list) {
+        const double v = row[J];
+        if (std::fabs(v) > truncation) {
+          out_cols.push_back(J);
+          out_vals.push_back(v);
+        }
+        row[J] = 0.0;
+        touched[J] = 0;
+      }
+      touched_list.clear();
+  }
+};
 
 }  // namespace
 
@@ -92,78 +179,25 @@ int ttg_host_assemble_hloc(const int* r, const double* MX, const double* MY,
   }
   const bool fill = (vals != nullptr);
   const double prune = truncation * 1e-6;
+  RowBuilder rb{rx, ry, rz, N, &sMX, &sMY, &sMZ, &sDX, &sDY, &sDZ, &sPX, &sPY, &sPZ, nterm, coef,
+                truncation, prune};
 
 #pragma omp parallel
   {
-    std::vector<double> row(N, 0.0);
-    std::vector<char> touched(N, 0);
-    std::vector<int> touched_list;
-    touched_list.reserve(1 << 16);
-    auto add = [&](int64_t J, double v) {
-      if (!touched[J]) {
-        touched[J] = 1;
-        touched_list.push_back((int)J);
-      }
-      row[J] += v;
-    };
+    RowScratch sc(N);
+    std::vector<int> cols;
+    std::vector<double> vs;
 #pragma omp for schedule(dynamic, 64)
     for (int64_t I = 0; I < N; ++I) {
-      const int xI = (int)(I % rx);
-      const int yI = (int)((I / rx) % ry);
-      const int zI = (int)(I / ((int64_t)rx * ry));
-      // kinetic: 0.5*(DX MY MZ + MX DY MZ + MX MY DZ)
-      const Sparse1D* A[3][3] = {{&sDX, &sMY, &sMZ}, {&sMX, &sDY, &sMZ}, {&sMX, &sMY, &sDZ}};
-      for (int term = 0; term < 3; ++term) {
-        const Sparse1D &ax = *A[term][0], &ay = *A[term][1], &az = *A[term][2];
-        for (int64_t pz = az.ptr[zI]; pz < az.ptr[zI + 1]; ++pz) {
-          const int zJ = az.col[pz];
-          const double vz = 0.5 * az.val[pz];
-          for (int64_t py = ay.ptr[yI]; py < ay.ptr[yI + 1]; ++py) {
-            const int yJ = ay.col[py];
-            const double vyz = vz * ay.val[py];
-            const int64_t base = (int64_t)rx * (yJ + (int64_t)ry * zJ);
-            for (int64_t px = ax.ptr[xI]; px < ax.ptr[xI + 1]; ++px)
-              add(base + ax.col[px], vyz * ax.val[px]);
-          }
-        }
+      cols.clear();
+      vs.clear();
+      rb.row(I, sc, cols, vs);
+      if (fill) {
+        std::copy(cols.begin(), cols.end(), col + row_ptr[I]);
+        std::copy(vs.begin(), vs.end(), vals + row_ptr[I]);
+      } else {
+        row_ptr[I + 1] = (int64_t)cols.size();
       }
-      // potential: sum_t coef_t PX_t PY_t PZ_t
-      for (int t = 0; t < nterm; ++t) {
-        const Sparse1D &px = sPX[t], &py = sPY[t], &pz = sPZ[t];
-        const double bound = std::fabs(coef[t]) * px.rowmax[xI] * py.rowmax[yI] * pz.rowmax[zI];
-        if (bound <= prune) continue;
-        for (int64_t qz = pz.ptr[zI]; qz < pz.ptr[zI + 1]; ++qz) {
-          const int zJ = pz.col[qz];
-          const double wz = coef[t] * pz.val[qz];
-          if (std::fabs(wz) * py.rowmax[yI] * px.rowmax[xI] <= prune) continue;
-          for (int64_t qy = py.ptr[yI]; qy < py.ptr[yI + 1]; ++qy) {
-            const int yJ = py.col[qy];
-            const double w = wz * py.val[qy];
-            if (std::fabs(w) * px.rowmax[xI] <= prune) continue;
-            const int64_t base = (int64_t)rx * (yJ + (int64_t)ry * zJ);
-            for (int64_t qx = px.ptr[xI]; qx < px.ptr[xI + 1]; ++qx)
-              add(base + px.col[qx], w * px.val[qx]);
-          }
-        }
-      }
-      std::sort(touched_list.begin(), touched_list.end());
-      int64_t cnt = 0;
-      int64_t out = fill ? row_ptr[I] : 0;
-      for (int J : touched_list) {
-        const double v = row[J];
-        if (std::fabs(v) > truncation) {
-          if (fill) {
-            col[out] = J;
-            vals[out] = v;
-            ++out;
-          }
-          ++cnt;
-        }
-        row[J] = 0.0;
-        touched[J] = 0;
-      }
-      touched_list.clear();
-      if (!fill) row_ptr[I + 1] = cnt;
     }
   }
   if (!fill) {
@@ -172,6 +206,72 @@ int ttg_host_assemble_hloc(const int* r, const double* MX, const double* MY,
   }
   return 0;
 }
+
+// ttg_host_assemble_hloc in one pass: every row is built once, into per-chunk
+// buffers, then copied into col_out / val_out (malloc'ed here, released with
+// ttg_host_free).  row_ptr: N + 1 entries, filled.
+int ttg_host_assemble_hloc_once(const int* r, const double* MX, const double* MY,
+                                const double* MZ, const double* DX, const double* DY,
+                                const double* DZ, int nterm, const double* coef,
+                                const double* PX, const double* PY, const double* PZ,
+                                double truncation, double drop, int64_t* row_ptr,
+                                int** col_out, double** val_out) {
+  if (!r || r[0] <= 0 || r[1] <= 0 || r[2] <= 0 || nterm < 0 || !row_ptr || !col_out ||
+      !val_out)
+    return -1;
+  const int rx = r[0], ry = r[1], rz = r[2];
+  const int64_t N = (int64_t)rx * ry * rz;
+  Sparse1D sMX = make_sparse(MX, rx, drop), sMY = make_sparse(MY, ry, drop),
+           sMZ = make_sparse(MZ, rz, drop);
+  Sparse1D sDX = make_sparse(DX, rx, drop), sDY = make_sparse(DY, ry, drop),
+           sDZ = make_sparse(DZ, rz, drop);
+  std::vector<Sparse1D> sPX(nterm), sPY(nterm), sPZ(nterm);
+  for (int t = 0; t < nterm; ++t) {
+    sPX[t] = make_sparse(PX + (int64_t)t * rx * rx, rx, drop);
+    sPY[t] = make_sparse(PY + (int64_t)t * ry * ry, ry, drop);
+    sPZ[t] = make_sparse(PZ + (int64_t)t * rz * rz, rz, drop);
+  }
+  RowBuilder rb{rx, ry, rz, N, &sMX, &sMY, &sMZ, &sDX, &sDY, &sDZ, &sPX, &sPY, &sPZ, nterm, coef,
+                truncation, truncation * 1e-6};
+  const int64_t chunk = 256, nchunks = (N + chunk - 1) / chunk;
+  std::vector<std::vector<int>> ccol(nchunks);
+  std::vector<std::vector<double>> cval(nchunks);
+#pragma omp parallel
+  {
+    RowScratch sc(N);
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t c = 0; c < nchunks; ++c) {
+      for (int64_t I = c * chunk; I < std::min(N, (c + 1) * chunk); ++I) {
+        const size_t before = ccol[c].size();
+        rb.row(I, sc, ccol[c], cval[c]);
+        row_ptr[I + 1] = (int64_t)(ccol[c].size() - before);
+      }
+    }
+  }
+  row_ptr[0] = 0;
+  for (int64_t I = 0; I < N; ++I) row_ptr[I + 1] += row_ptr[I];
+  const int64_t nnz = row_ptr[N];
+  int* col = static_cast<int*>(std::malloc(std::max<int64_t>(nnz, 1) * sizeof(int)));
+  double* vals = static_cast<double*>(std::malloc(std::max<int64_t>(nnz, 1) * sizeof(double)));
+  if (!col || !vals) {
+    std::free(col);
+    std::free(vals);
+    return -2;
+  }
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t c = 0; c < nchunks; ++c) {
+    const int64_t o = row_ptr[c * chunk];
+    std::copy(ccol[c].begin(), ccol[c].end(), col + o);
+    std::copy(cval[c].begin(), cval[c].end(), vals + o);
+    std::vector<int>().swap(ccol[c]);
+    std::vector<double>().swap(cval[c]);
+  }
+  *col_out = col;
+  *val_out = vals;
+  return 0;
+}
+
+void ttg_host_free(void* p) { std::free(p); }
 
 // Separable nonlocal projector matrix C (nproj x N, CSR):
 //   C[a, J] = cx[a, xJ] * cy[a, yJ] * cz[a, zJ], kept where |C| > tol.

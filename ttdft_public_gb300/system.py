@@ -261,19 +261,20 @@ def assemble_hloc(basis, coef, fx, fy, fz, truncation) -> tuple[Csr, dict]:
     coef = np.ascontiguousarray(coef, dtype=np.float64)
     P = [np.ascontiguousarray(a, dtype=np.float64) for a in (PX, PY, PZ)]
     ptr = _lib.ptr
-    rc = lib.ttg_host_assemble_hloc(ptr(r), *[ptr(a) for a in args], nterm, ptr(coef),
-                                    *[ptr(a) for a in P], ctypes.c_double(truncation),
-                                    ctypes.c_double(1e-15), ptr(row_ptr), None, None)
+    cp, vp = ctypes.c_void_p(), ctypes.c_void_p()
+    rc = lib.ttg_host_assemble_hloc_once(ptr(r), *[ptr(a) for a in args], nterm, ptr(coef),
+                                         *[ptr(a) for a in P], ctypes.c_double(truncation),
+                                         ctypes.c_double(1e-15), ptr(row_ptr), ctypes.byref(cp),
+                                         ctypes.byref(vp))
     if rc != 0:
         raise RuntimeError(f"H_loc assembly failed ({rc})")
     nnz = int(row_ptr[-1])
-    col = np.zeros(nnz, dtype=np.int32)
-    val = np.zeros(nnz, dtype=np.float64)
-    rc = lib.ttg_host_assemble_hloc(ptr(r), *[ptr(a) for a in args], nterm, ptr(coef),
-                                    *[ptr(a) for a in P], ctypes.c_double(truncation),
-                                    ctypes.c_double(1e-15), ptr(row_ptr), ptr(col), ptr(val))
-    if rc != 0:
-        raise RuntimeError(f"H_loc assembly failed ({rc})")
+    try:
+        col = np.ctypeslib.as_array(ctypes.cast(cp, ctypes.POINTER(ctypes.c_int32)), (max(nnz, 1),))[:nnz].copy()
+        val = np.ctypeslib.as_array(ctypes.cast(vp, ctypes.POINTER(ctypes.c_double)), (max(nnz, 1),))[:nnz].copy()
+    finally:
+        lib.ttg_host_free(cp)
+        lib.ttg_host_free(vp)
     mats = dict(MX=MX, MY=MY, MZ=MZ, DX=DX, DY=DY, DZ=DZ, PX=PX, PY=PY, PZ=PZ, coef=coef)
     return Csr(N, N, row_ptr, col, val), mats
 
