@@ -45,6 +45,13 @@ METRIC = "s/SCF-iter & time-to-SCF @\u0394E<1e-5 Ha/atom: mixed+learned vs FP64,
 WORKLOAD = "atoms64"
 MIX_ALPHA = 0.1          # Anderson mixing parameter of this workload (input parameter)
 MIX_DEPTH = 10           # Anderson history (the reference example's history=10)
+# per-workload SCF settings: the 512-atom run keeps the configuration's
+# Anderson depth of 5 (its 720^3 FP64 fields are 3 GB each) and Tucker ranks
+# scaled with the 8x larger box
+SCF_SETTINGS = {
+    "atoms64": {},
+    "atoms512": {"history": 5, "rho_rank_cap": 96, "veff_rank_cap": 120, "rho_out_rank_cap": 160},
+}
 # DRAM bytes per 128-row column slot of one FP32 filter degree (k_cheb_umma),
 # measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass) on
 # the 64-atom operator with its 160-column block (profile_workload --workload
@@ -148,13 +155,15 @@ def max_over_ranks(x, world):
 def make_system():
     from ttdft_public_gb300 import system
     cache = os.environ.get("TTG_CACHE", os.path.join(ROOT, "_build", "systems"))
+    if WORKLOAD == "atoms512":
+        cache = None            # 14 GB of H: rebuilt rather than written to disk
     return system.build_system(system.CONFIGS[WORKLOAD], cache_dir=cache)
 
 
 def scf_config(filt, **kw):
     from ttdft_public_gb300 import scf
-    return scf.ScfConfig(filter=filt, mix_alpha=MIX_ALPHA, history=MIX_DEPTH, max_iter=MAX_ITER,
-                         **kw)
+    opts = {"history": MIX_DEPTH, **SCF_SETTINGS.get(WORKLOAD, {}), **kw}
+    return scf.ScfConfig(filter=filt, mix_alpha=MIX_ALPHA, max_iter=MAX_ITER, **opts)
 
 
 class Timer:
@@ -247,38 +256,40 @@ def run_ours(args, rank, world):
         roof[kind] = {"launch_ms": per * 1e3, "launches": cnt, "bytes_per_launch": bytes_deg,
                       "flops_per_launch": 2.0 * nnz * k, "achieved": bytes_deg / per / 1e9}
     op.kernel_timing(False)
-    g.close()
-    del g, it
+    it.close()
+    rho_host = g.rho.cpu().numpy() if rank == 0 else None
 
     # ---- end to end: the same iterations with the densities held on the host
-    # (measured right after the device-timed run, with the same device state)
-    g3 = scf.Scf(s, scf_config("mixed"))
-    it3 = g3.iterate(max_iter=args.warmup + args.steps, tol=0.0, host_io=True)
+    # (right after the device-timed run, same operator, from the same start)
+    it3 = g.iterate(max_iter=args.warmup + args.steps, tol=0.0, host_io=True)
     for _ in range(args.warmup):
         next(it3)
     with Timer() as te:
         recs3 = [next(it3) for _ in range(args.steps)]
     e2e = max_over_ranks(te.s, world) / args.steps
-    nq = g3.nq
+    nq = g.nq
     p3 = float(np.mean([r["passes"] for r in recs3]))
-    g3.close()
-    del g3, it3
+    it3.close()
+    g.close()
+    del g, it, it3
 
     # ---- time to SCF: mixed, FP64, learned initial guess
     tts = {}
-    tts["mixed"], gm = time_to_scf(s, "mixed")
-    log("time to SCF, mixed:", tts["mixed"])
-    rho_host = gm.rho.cpu().numpy() if rank == 0 else None
-    gm.close()
-    del gm
-    if not args.no_fp64:
+    do_tts = args.tts if args.tts is not None else WORKLOAD == "atoms64"
+    if do_tts:
+        tts["mixed"], gm = time_to_scf(s, "mixed")
+        log("time to SCF, mixed:", tts["mixed"])
+        rho_host = gm.rho.cpu().numpy() if rank == 0 else None
+        gm.close()
+        del gm
+    if do_tts and not args.no_fp64:
         tts["fp64"], g64 = time_to_scf(s, "fp64")
         log("time to SCF, fp64:", tts["fp64"])
         g64.close()
         del g64
         tts["fp64"]["de_atom_vs_mixed"] = abs(tts["fp64"]["energy_ha"] - tts["mixed"]["energy_ha"]) / s.spec.n_atoms
     from ttdft_public_gb300 import learned
-    if learned.load_default() is not None:
+    if do_tts and learned.load_default() is not None:
         tts["mixed_learned"], gl = time_to_scf(s, "mixed", guess="learned")
         gl.close()
         del gl
@@ -306,8 +317,9 @@ def run_ours(args, rank, world):
                        "quad_points": int(nq), "anderson_depth": MIX_DEPTH, "mix_alpha": MIX_ALPHA,
                        "nnz_per_row": info["nnz_h"] / n, "nproj": s.C.n_rows,
                        "passes_per_iter": passes, "iters_timed": [r["iter"] for r in recs],
-                       "l2": "inputs larger than L2: H %.2f GB on the device, 360^3 FP64 "
-                             "fields of 373 MB" % (info["device_bytes"] / 1e9),
+                       "l2": "inputs larger than L2: H %.2f GB on the device, %d^3 FP64 "
+                             "fields of %.0f MB" % (info["device_bytes"] / 1e9,
+                                                    round(nq ** (1 / 3)), nq * 8 / 1e6),
                        "parallelism": f"replicas x{world}", "system_gen_s": round(gen_s, 1)},
             "time_to_scf": tts,
             "roofline": {"bound": "hbm", "kernel": kname,
@@ -359,7 +371,8 @@ def log(*a):
 def cpu_baseline(s, passes, rho_host, g, scale=True):
     """Oracle (FP64, all host threads) on a bounded sample of one SCF
     iteration of this workload: two filter degrees + one H application on the
-    full block, one fixed-rank STHOSVD of the 360^3 density and 3 of the 35
+    block (its first 64 columns when wider than 256), one fixed-rank STHOSVD
+    of the density and 3 of the 35
     Hartree terms; scaled to passes x (degree + 1) H applications, two
     STHOSVDs and two 35-term Hartree evaluations per iteration (the H update,
     density and grid pointwise work are not counted)."""
@@ -367,11 +380,14 @@ def cpu_baseline(s, passes, rho_host, g, scale=True):
     from oracle import scf as oscf
     from ttdft_public_gb300.kernel_expansion import coulomb_expansion
     k, m = s.spec.n_states, s.spec.degree
-    X = np.random.default_rng(1).standard_normal((s.N, k))
+    # the H application's cost is linear in the block width: wide blocks are
+    # sampled on their first 64 columns and scaled
+    kc = min(k, 64) if k > 256 else k
+    X = np.random.default_rng(1).standard_normal((s.N, kc))
     t = time.perf_counter()
     oracle.cheb_filter(s, X, m, 0.0, 30.0, -0.5, steps_limit=2)
     oracle.apply_h(s, X)
-    t_apply = (time.perf_counter() - t) / 3.0
+    t_apply = (time.perf_counter() - t) / 3.0 * k / kc
     q = [b.fem.nq for b in s.basis]
     rho = rho_host.reshape(q[2], q[1], q[0])
     t = time.perf_counter()
@@ -383,12 +399,13 @@ def cpu_baseline(s, passes, rho_host, g, scale=True):
     oracle.hartree(alpha[:3], omega[:3], np.transpose(core, (2, 1, 0)), quad, U,
                    [b.fem.xq for b in s.basis])
     t_h = (time.perf_counter() - t) * len(alpha) / 3.0
-    sample = 3 * t_apply + t_sth + t_h * 3.0 / len(alpha)
+    sample = 3 * t_apply * kc / k + t_sth + t_h * 3.0 / len(alpha)
     est = passes * (m + 1) * t_apply + 2 * t_sth + 2 * t_h
     return {"value": est, "unit": "s/SCF-iter", "cores": oracle.threads(), "kind": "port",
             "sample": f"{sample:.1f} s of FP64 CPU work on the {WORKLOAD} data: 2 filter degrees "
-                      f"+ 1 H application ({t_apply:.2f} s per application), one rank-60 STHOSVD "
-                      f"of the 360^3 density ({t_sth:.2f} s), 3 of 35 Hartree terms; scaled to "
+                      f"+ 1 H application on {kc} of {k} columns ({t_apply:.2f} s per "
+                      f"{k}-column application), one rank-60 STHOSVD of the {q[0]}^3 density "
+                      f"({t_sth:.2f} s), 3 of 35 Hartree terms; scaled to "
                       f"{passes:.1f} passes x {m + 1} applications + 2 STHOSVD + 2 Hartree per "
                       f"iteration (H update, density, pointwise grid work not counted)"}
 
@@ -443,7 +460,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 time-to-SCF run")
+    ap.add_argument("--workload", default="atoms64", choices=["atoms64", "atoms512"])
+    ap.add_argument("--tts", dest="tts", action="store_true", default=None,
+                    help="time-to-SCF runs (default: on for atoms64, off for atoms512)")
+    ap.add_argument("--no-tts", dest="tts", action="store_false")
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = args.workload
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
