@@ -167,8 +167,14 @@ ttg_status ttg_op_create_tucker(int64_t n, const int64_t* h_row_ptr, const int32
   const char* dis = getenv("TTG_DISABLE_TC");
   op->tc_disabled = dis && dis[0] == '1';
   if (!op->tc_disabled) {
-    s = build_tiles(op, n, h_row_ptr, h_col, h_val, nproj, c_row_ptr, c_col, c_val, tucker_ranks);
-    if (s != TTG_OK) return fail(s);
+    // the mma.sync tiles serve block widths that are not multiples of 16;
+    // an op for wide blocks of multiples of 16 (the tcgen05 degrees run them
+    // in column blocks) does without them and their memory
+    if (!(max_k > 256 && max_k % 16 == 0)) {
+      s = build_tiles(op, n, h_row_ptr, h_col, h_val, nproj, c_row_ptr, c_col, c_val,
+                      tucker_ranks);
+      if (s != TTG_OK) return fail(s);
+    }
     s = build_umma_tiles(op, n, h_row_ptr, h_col, h_val, nproj, c_row_ptr, c_col, c_val,
                          tucker_ranks);
     if (s != TTG_OK) return fail(s);
