@@ -205,6 +205,7 @@ ttg_status ttg_op_destroy(ttg_op* op) {
                     &op->tiles.tptr, &op->tiles.tcol, &op->tiles.rowmap, &op->tiles.v32,
                     &op->tiles.v16, &op->pattern.row_ptr, &op->pattern.col,
                     &op->pattern.rg_pos, &op->pattern.tile_base, &op->pattern.tile_slot,
+                    &op->pattern.umma_pos, &op->pattern.umma_row,
                     &op->pattern.kin, &op->pattern.work, &op->pattern.work2};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < kMaxSlots; ++i)

@@ -46,8 +46,11 @@ struct UpdateArgs {
   __nv_bfloat16* v16;
   float* t32;
   __nv_bfloat16* t16;
-  const int* umma_pos;        // element of the entry in plane 0 of the 128-row tiles
-  __nv_bfloat16* u16;         // their three BF16 planes (2048 elements apart)
+  const int64_t* rg_gptr;     // slot offset of each row group
+  const int* umma_pos;        // slot of the entry within its 128-row tile
+  const int* umma_row;        // tile * 128 + lane of each row
+  const int64_t* umma_tptr;   // slot offset of each tile (multiples of 16)
+  __nv_bfloat16* u16;         // the tiles' three BF16 planes (2048 elements apart)
   int64_t n;
 };
 
@@ -96,7 +99,8 @@ __global__ void k_update_values(UpdateArgs a) {
       for (; c < a.rc; ++c) s0 = fma(pz[c], t2[c], s0);
       val += (s0 + s1) + (s2 + s3);
     }
-    const int p = a.rg_pos[e];
+    // value index in the row groups: (group slot offset + slot) * 8 + row in group
+    const int64_t p = (a.rg_gptr[row >> 3] + a.rg_pos[e]) * 8 + (row & 7);
     a.v64[p] = val;
     if (a.vdf) {
       const float h = __double2float_rn(val);
@@ -114,7 +118,14 @@ __global__ void k_update_values(UpdateArgs a) {
     }
     if (a.u16) {
       // three BF16 terms, as the tile builder splits them
-      __nv_bfloat16* u = a.u16 + a.umma_pos[e];
+      // element in plane 0: chunk (tile's first + slot / 16), canonical K-major
+      // position of (lane, slot % 16) within the chunk's 128 x 16 plane
+      const int ur = a.umma_row[row];
+      const int m = ur & 127, sl = a.umma_pos[e];
+      const int64_t chunk = a.umma_tptr[ur >> 7] / 16 + (sl >> 4);
+      const int s16 = sl & 15;
+      __nv_bfloat16* u = a.u16 + chunk * 6144 + ((m >> 3) * 128 + (s16 >> 3) * 64 + (m & 7) * 8 +
+                                                 (s16 & 7));
       const __nv_bfloat16 h0 = __float2bfloat16_rn((float)val);
       const double r1 = val - (double)__bfloat162float(h0);
       const __nv_bfloat16 h1 = __float2bfloat16_rn((float)r1);
@@ -212,7 +223,10 @@ ttg_status update_from_tables(ttg_op* op, const UpdateLayout& L) {
   a.v16 = op->rg.v16.as<__nv_bfloat16>();
   a.t32 = op->tiles.n_tiles > 0 && P.tile_base.p ? op->tiles.v32.as<float>() : nullptr;
   a.t16 = op->tiles.v16.as<__nv_bfloat16>();
+  a.rg_gptr = op->rg.gptr.as<int64_t>();
   a.umma_pos = P.umma_pos.as<int>();
+  a.umma_row = P.umma_row.as<int>();
+  a.umma_tptr = op->umma.tptr.as<int64_t>();
   a.u16 = op->umma.n_tiles > 0 && P.umma_pos.p ? op->umma.hpl.as<__nv_bfloat16>() : nullptr;
   a.n = op->n;
   const int wpb = 8;

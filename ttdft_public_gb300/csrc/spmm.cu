@@ -558,7 +558,7 @@ ttg_status build_row_groups(ttg_op* op, int64_t n, const int64_t* hp, const int3
         for (int64_t e = hp[r]; e < hp[r + 1]; ++e) {
           while (cols[s] != hc[e]) ++s;
           gval[(base + s) * G + (r - r0)] = hv[e];
-          if (!rgpos.empty()) rgpos[e] = (int32_t)((base + s) * G + (r - r0));
+          if (!rgpos.empty()) rgpos[e] = (int32_t)s;   // slot within the group
         }
         if (nproj > 0)
           for (int64_t e = tp[r]; e < tp[r + 1]; ++e) {

@@ -573,7 +573,6 @@ ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int3
   const int64_t slots = tptr[ntiles];
   const int64_t nchunk = slots / UK;
   const bool keep = op->keep_pattern;
-  if (nchunk * (int64_t)CHUNK_ELEMS >= INT32_MAX && keep) return TTG_OK;   // no map possible
   std::vector<int32_t> tcol(std::max<int64_t>(slots, UK), 0);
   std::vector<uint16_t> hpl((size_t)std::max<int64_t>(nchunk, 1) * CHUNK_ELEMS, 0);
   std::vector<int32_t> pos(keep ? hp[n] : 0);
@@ -600,7 +599,7 @@ ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int3
             uint16_t tt[3];
             split3_host(V[e], tt);
             for (int p = 0; p < 3; ++p) hpl[base + p * PLANE_ELEMS] = tt[p];
-            if (keep && pass == 0) pos[hp[r] + e] = (int32_t)base;
+            if (keep && pass == 0) pos[hp[r] + e] = (int32_t)slot;   // slot within the tile
           }
         }
       }
@@ -627,7 +626,15 @@ ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int3
     TTG_TRY(op->pattern.umma_pos.alloc(hp[n] * sizeof(int32_t)));
     TTG_CUDA_TRY(cudaMemcpyAsync(op->pattern.umma_pos.p, pos.data(), hp[n] * sizeof(int32_t),
                                  cudaMemcpyHostToDevice, op->stream));
-    op->device_bytes += op->pattern.umma_pos.bytes;
+    // row -> tile * 128 + lane of the row in its tile
+    std::vector<int32_t> urow(n, -1);
+    for (int64_t t = 0; t < ntiles; ++t)
+      for (int m = 0; m < UR; ++m)
+        if (rowmap[t * UR + m] >= 0) urow[rowmap[t * UR + m]] = (int32_t)(t * UR + m);
+    TTG_TRY(op->pattern.umma_row.alloc(n * sizeof(int32_t)));
+    TTG_CUDA_TRY(cudaMemcpyAsync(op->pattern.umma_row.p, urow.data(), n * sizeof(int32_t),
+                                 cudaMemcpyHostToDevice, op->stream));
+    op->device_bytes += op->pattern.umma_pos.bytes + op->pattern.umma_row.bytes;
   }
   TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
   op->device_bytes += U.tptr.bytes + U.tcol.bytes + U.rowmap.bytes + U.order.bytes + U.hpl.bytes;

@@ -132,10 +132,11 @@ struct UmmaOp {
 struct Pattern {
   DevBuf row_ptr;    // int64 [n+1]
   DevBuf col;        // int32 [nnz]
-  DevBuf rg_pos;     // int32 [nnz]: index into the row-group value arrays
+  DevBuf rg_pos;     // int32 [nnz]: slot of the entry within its row group's column list
   DevBuf tile_base;  // int32 [nnz]: lane base of the entry's tile fragment
   DevBuf tile_slot;  // uint8 [nnz]: slot of the entry within its 16-slot chunk
-  DevBuf umma_pos;   // int32 [nnz]: element of the entry in plane 0 of the 128-row tiles
+  DevBuf umma_pos;   // int32 [nnz]: slot of the entry within its 128-row tile's column list
+  DevBuf umma_row;   // int32 [n]: tile * 128 + lane of each row in the 128-row tiles
   int32_t r[3] = {0, 0, 0};   // Tucker ranks of the basis
   int32_t bw[3] = {0, 0, 0};  // max |coordinate difference| per direction over the entries
   DevBuf kin;        // 6 r x r 1-D matrices: DX DY DZ MX MY MZ (row-major)
