@@ -177,19 +177,6 @@ __device__ __forceinline__ int grid_exp(float amax) {
   return e;
 }
 
-// round to the nearest integer (ties to even) for |x| < 2^22 on the FMA
-// pipe: adding and subtracting 1.5 * 2^23 drops the fraction
-__device__ __forceinline__ float rint_fma(float x) {
-  const float big = 12582912.f;
-  return __fsub_rn(__fadd_rn(x, big), big);
-}
-
-// two integers |v| <= 256 as a BF16 pair: BF16 is the upper half of FP32, and
-// these values have no bits below it, so the halves are moved, not rounded
-__device__ __forceinline__ uint32_t bf16x2_exact(float lo, float hi) {
-  return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
-}
-
 // three integer slices of 8 values on the grid 2^(e-8): v 2^(8-e) = a0 + a1/256 + a2/65536
 __device__ __forceinline__ void slice8(const float* v, float sc, uint4& p0, uint4& p1,
                                        uint4& p2) {
@@ -200,14 +187,17 @@ __device__ __forceinline__ void slice8(const float* v, float sc, uint4& p0, uint
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const float x = v[2 * j + h] * sc;          // |x| < 256, exact (power-of-two scale)
-      a[h] = rint_fma(x);
+      a[h] = rintf(x);
       const float r = (x - a[h]) * 256.f;         // exact, |r| <= 128
-      b[h] = rint_fma(r);
-      c[h] = rint_fma((r - b[h]) * 256.f);
+      b[h] = rintf(r);
+      c[h] = rintf((r - b[h]) * 256.f);
     }
-    w0[j] = bf16x2_exact(a[0], a[1]);
-    w1[j] = bf16x2_exact(b[0], b[1]);
-    w2[j] = bf16x2_exact(c[0], c[1]);
+    const __nv_bfloat162 h0 = __floats2bfloat162_rn(a[0], a[1]);   // integers <= 256: exact
+    const __nv_bfloat162 h1 = __floats2bfloat162_rn(b[0], b[1]);
+    const __nv_bfloat162 h2 = __floats2bfloat162_rn(c[0], c[1]);
+    w0[j] = *reinterpret_cast<const uint32_t*>(&h0);
+    w1[j] = *reinterpret_cast<const uint32_t*>(&h1);
+    w2[j] = *reinterpret_cast<const uint32_t*>(&h2);
   }
   p0 = make_uint4(w0[0], w0[1], w0[2], w0[3]);
   p1 = make_uint4(w1[0], w1[1], w1[2], w1[3]);
