@@ -115,12 +115,12 @@ def test_hartree_energy_matches_oracle(gpu_scf, cpu_scf):
 def test_scf_iterations_match_oracle(scf_system):
     """The FP64 GPU loop against the oracle loop, iteration by iteration.
 
-    The GPU computes V_H (the kernel-expansion contraction) in FP32 with a
-    3-term TF32 split: 5e-7 relative to max |V_H| on this system, which moves
-    eigenvalues by ~6e-6 Ha.  Energies of the first iterations (far from
-    self-consistency, where the energy is not stationary in V_in) therefore
-    agree to ~1e-5 Ha; the Hartree energy itself is FP64-exact, so the
-    converged energies agree to ~1e-8 Ha.  Same iteration count required."""
+    The GPU computes V_H from FP32 operands on the tensor cores (exact
+    integer slicing, ~1e-7 of max |V_H| on this system); energies of the
+    first iterations (far from self-consistency, where the energy is not
+    stationary in V_in) agree within the stated bound, and the Hartree energy
+    itself is FP64-exact, so the converged energies agree to ~1e-8 Ha.  Same
+    iteration count required."""
     run_g = scf.Scf(scf_system, cfg()).run()
     run_c = oscf.OracleScf(scf_system, cfg()).run()
     eg = np.array([h["energy"] for h in run_g["history"]])
