@@ -610,7 +610,6 @@ ttg_status build_row_groups(ttg_op* op, int64_t n, const int64_t* hp, const int3
   op->nnz_h = hp[n];
   op->nnz_c = C.nnz;
   if (op->keep_pattern && hp[n] > 0) {
-    if (slots * G >= INT32_MAX) return TTG_BAD_ARG;
     Pattern& P = op->pattern;
     // half-bandwidth of the pattern in each Tucker direction
     const int rx = P.r[0], ry = P.r[1];
