@@ -310,7 +310,7 @@ def run_ours(args, rank, world):
             "metric": METRIC, "value": sec_per_iter, "unit": "s/SCF-iter", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_iter * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16/fp32 filter, fp64 Rayleigh-Ritz, 3xTF32 Hartree, fp64 grids",
+            "dtype": "bf16/fp32 filter, fp64 Rayleigh-Ritz (double-fp32 arithmetic), exact-sliced bf16 tensor-core Hartree and density, fp64 grids",
             "data": "synthetic (seeded atoms)",
             "config": {"workload": f"{WORKLOAD}: full SCF iteration (mixed filter)",
                        "N": n, "states": k, "degree": m, "bf16_degrees": m // 4,

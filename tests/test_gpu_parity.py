@@ -288,8 +288,29 @@ def test_density_matches_oracle(small_op, small_system):
     occ = np.linspace(1.0, 0.0, 24)
     rho = api.density(small_op, api.Mat(small_op, 24, X), occ, s.basis)
     ref = oracle.density(X, occ, s.basis)
-    # FP32 tensor-core mode products (3-term TF32 split), FP32 accumulation
+    # exact-sliced tensor-core mode products on FP32 operands, the states
+    # summed in double-FP32
     assert np.linalg.norm(rho - ref) / np.linalg.norm(ref) < 1e-6
+
+
+def test_density_in_chunks_of_states(small_op, small_system, monkeypatch):
+    """A scratch budget of five states' intermediates splits the 24 states
+    into five chunks (the last one short), each accumulated into the same
+    FP64 density: the result matches the oracle and the one-chunk build."""
+    s = small_system
+    X, _ = oracle.cholqr(np.random.default_rng(11).standard_normal((s.N, 24)))
+    occ = np.linspace(1.0, 0.0, 24)
+    Xd = api.Mat(small_op, 24, X)
+    whole = api.density(small_op, Xd, occ, s.basis)
+    r = [b.r for b in s.basis]
+    n = [b.nodal.shape[0] for b in s.basis]
+    rp = [(x + 3) // 4 * 4 for x in r]
+    per_state = (r[1] * r[2] * rp[0] + r[2] * n[0] * rp[1] + n[1] * n[0] * rp[2]) * 4
+    monkeypatch.setenv("TTG_DENSITY_CHUNK_BYTES", str(5 * per_state))
+    parts = api.density(small_op, Xd, occ, s.basis)
+    ref = oracle.density(X, occ, s.basis)
+    assert np.linalg.norm(parts - ref) / np.linalg.norm(ref) < 1e-6
+    assert np.linalg.norm(parts - whole) / np.linalg.norm(whole) < 1e-12
 
 
 def hartree_case(seed=0, r=(12, 10, 8), nq=(40, 36, 30), n=(33, 31, 29), K=7):

@@ -221,17 +221,20 @@ ttg_status hartree_tc(cudaStream_t st, HartreeWork& w, const HartreeIn& in, doub
   TOperand B1{w.F[0].as<float>(), nx, rx, rxp, K, (int64_t)nx * rxp, am_f[0]};
   TOut o1{w.p2.p, ry, 1, ryp, (int64_t)rz * ryp, (int64_t)nx * rz * ryp};
   o1.omax = am_p;
+  o1.limit = (int64_t)K * nx * rz * ryp;
   TTG_TRY(tgemm(st, TG_STORE_F32, A1, B1, K, 1, (int)((rx + 15) / 16), o1, err));
   // 2) Q[(i + nx j)][(t, c)] = sum_b P_t[(i, c)][b] Fy_t[j][b]   rows (i, c) x cols j, batch t
   TOperand A2{w.p2.as<float>(), (int64_t)nx * rz, ry, ryp, K, (int64_t)nx * rz * ryp, am_p};
   TOperand B2{w.F[1].as<float>(), ny, ry, ryp, K, (int64_t)ny * ryp, am_f[1]};
   TOut o2{w.q.p, rz, 1, kt, (int64_t)nx * kt, ktt};
   o2.omax = am_q;
+  o2.limit = qrows * kt;
   TTG_TRY(tgemm(st, TG_STORE_F32, A2, B2, K, 1, (int)((ry + 15) / 16), o2, err));
   // 3) V[(i, j), l] = sum_t sum_c Q[(i, j)][(t, c)] w_t Fz_t[l][c], one group per term
   TOperand A3{w.q.as<float>(), qrows, kt, kt, 0, 0, am_q};
   TOperand B3{w.F[2].as<float>(), nz, kt, kt, 0, 0, am_f[2]};
   TOut o3{V, qrows + 1, 1, 0, qrows, 0};
+  o3.limit = qrows * nz;
   TTG_TRY(tgemm(st, TG_SUM_F64, A3, B3, 1, K, (int)(ktt / 16), o3, err));
   if (e1) TTG_CUDA_TRY(cudaEventRecord(e1, st));
   return TTG_OK;
@@ -244,6 +247,14 @@ ttg_status hartree_check(HartreeWork& w, cudaStream_t st) {
   TTG_CUDA_TRY(cudaStreamSynchronize(st));
   if (e) {
     TTG_CUDA_TRY(cudaMemsetAsync(w.err.p, 0, sizeof(int), st));
+    if (e == 2) {
+      fprintf(stderr, "ttg: a tensor-core contraction skipped stores outside its output\n");
+      return TTG_BAD_ARG;
+    }
+    if (e == 3) {
+      fprintf(stderr, "ttg: a tensor-core contraction found a copy barrier out of phase\n");
+      return TTG_CUDA_ERR;
+    }
     return TTG_TIMEOUT;
   }
   return TTG_OK;
@@ -304,18 +315,21 @@ ttg_status density_tc(ttg_op* op, const ttg_block* X, const double* occ, int rx,
     TOperand B1{D.uf[0].as<float>(), nx, rx, rxp, 0, 0, dm};
     TOut o1{D.p1.p, ry, 1, (int64_t)nx * ryp, ryp, (int64_t)rz * nx * ryp};
     o1.omax = am_1;
+    o1.limit = (int64_t)sc * rz * nx * ryp;
     TTG_TRY(tgemm(st, TG_STORE_F32, A1, B1, sc, 1, (rx + 15) / 16, o1, err));
     // 2) P2[s][j][i][c] = sum_b P1[s][(c, i)][b] Uy[j][b]       rows (c, i), cols j, batch s
     TOperand A2{D.p1.as<float>(), (int64_t)rz * nx, ry, ryp, sc, (int64_t)rz * nx * ryp, am_1};
     TOperand B2{D.uf[1].as<float>(), ny, ry, ryp, 0, 0, dm + 1};
     TOut o2{D.p2.p, nx, rzp, 1, (int64_t)nx * rzp, (int64_t)ny * nx * rzp};
     o2.omax = am_2;
+    o2.limit = (int64_t)sc * ny * nx * rzp;
     TTG_TRY(tgemm(st, TG_STORE_F32, A2, B2, sc, 1, (ry + 15) / 16, o2, err));
     // 3) rho[(i, j), l] (+)= sum_s w_s (sum_c P2[s][(j, i)][c] Uz[l][c])^2
     TOperand A3{D.p2.as<float>(), (int64_t)nx * ny, rz, rzp, sc, (int64_t)ny * nx * rzp, am_2};
     TOperand B3{D.uf[2].as<float>(), nz, rz, rzp, 0, 0, dm + 2};
     TOut o3{rho, (int64_t)nx * ny + 1, 1, 0, (int64_t)nx * ny, 0, D.w.as<float>() + s0,
             (accumulate || s0 > 0) ? 1 : 0};
+    o3.limit = (int64_t)nx * ny * nz;
     TTG_TRY(tgemm(st, TG_SQSUM_F64, A3, B3, 1, sc, (rz + 15) / 16, o3, err));
     op->launches += 3;
   }

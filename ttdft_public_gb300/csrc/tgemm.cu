@@ -31,6 +31,11 @@
 //  - warp 0, one thread: TMA tiled loads (cp.async.bulk.tensor) of the FP32
 //    tiles A[128 rows][16] and B[48 rows][16] of one K-chunk into a raw
 //    ring; rows and K beyond the tensor's extent are filled with zeros;
+//  - warp 3, one thread: waits for the raw stages' copies in order and
+//    publishes the count of landed chunks.  The converter warps take chunks
+//    round-robin, so one polling a stage's barrier itself could meet it a
+//    phase early (the previous chunk of that stage, another warp's, still in
+//    flight) and read the stage's previous-but-one completion as its own;
 //  - warps 4-9, whole chunks in turn: slice the chunk's 176 rows into three
 //    BF16 planes each, written in the canonical K-major layout of the MMA
 //    operands (8-row x 16-byte core matrices), fence them for the async
@@ -139,6 +144,18 @@ __device__ __forceinline__ bool bar_drain(uint64_t* b, uint32_t parity) {
   return false;
 }
 
+// non-blocking: has the phase of this parity completed (is the barrier past it)?
+__device__ __forceinline__ bool bar_test(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 __device__ __forceinline__ void bar_arrive(uint64_t* b) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
 }
@@ -245,7 +262,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2];
   __shared__ __align__(8) uint64_t fin;                        // all MMAs issued have completed
   __shared__ uint32_t tmem_slot;
-  __shared__ uint32_t ready;
+  __shared__ uint32_t ready;                                   // chunks sliced
+  __shared__ uint32_t landed;                                  // chunks whose raw copies landed
   __shared__ int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t ntiles = (int64_t)sch.tiles_m * sch.tiles_n * Z;
@@ -276,6 +294,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
     }
     bar_init(&fin, 1);
     ready = 0;
+    landed = 0;
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -301,6 +320,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
           if (q >= kRawStages &&
               !bar_wait(&raw_empty[s], (uint32_t)((q / kRawStages - 1) & 1), abrt, 32)) {
             ok = false;
+            break;
+          }
+          // the stage's previous copy (chunk q - kRawStages) must have landed
+          // before this chunk's arrival: otherwise the arrival would fall into
+          // that phase.  Holds by construction; checked so that a broken
+          // invariant ends the kernel with an error, not with a bad barrier
+          if (q >= kRawStages && !bar_test(&raw_full[s], (uint32_t)((q / kRawStages - 1) & 1))) {
+            atomicExch(err, 3);
+            ok = false;
+            *abrt = 1;
             break;
           }
           const uint32_t fb = su32(&raw_full[s]);
@@ -331,7 +360,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
       const float scb = ldexpf(1.f, 8 - grid_exp(__ldg(amaxB + sidx_b(g, z))));
       bool w = true;
       if (lane == 0) {
-        w = bar_wait(&raw_full[s], (uint32_t)((q / kRawStages) & 1), abrt, 32);
+        // chunk q has landed (published in order by warp 3)
+        w = false;
+        for (int i = 0; i < kMaxWait; ++i) {
+          uint32_t l;
+          asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(l) : "r"(su32(&landed))
+                       : "memory");
+          if (l > (uint32_t)q) { w = true; break; }
+          if (*abrt) break;
+          __nanosleep(32);
+        }
+        if (!w) *abrt = 1;
         // the MMAs of chunk q - kSplitStages have read this slice stage
         if (w && q >= kSplitStages)
           w = bar_wait(&spl_empty[s2], (uint32_t)((q / kSplitStages - 1) & 1), abrt, 32);
@@ -366,6 +405,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
       if (lane == 0) {
         bar_arrive(&raw_empty[s]);
         bar_arrive(&spl_full[s2]);
+      }
+    }
+  } else if (warp == 3) {
+    // ---- waits for the raw copies in order; the converters read the count
+    if (lane == 0) {
+      const int64_t total = (int64_t)my_tiles * nk;
+      for (int64_t q = 0; q < total; ++q) {
+        if (!bar_wait(&raw_full[q % kRawStages], (uint32_t)((q / kRawStages) & 1), abrt, 32)) {
+          ok = false;
+          break;
+        }
+        asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"(su32(&landed)),
+                     "r"((uint32_t)(q + 1)) : "memory");
       }
     }
   } else if (warp == 2) {
@@ -460,6 +512,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
       const uint32_t hcol = tmem + lanes + (uint32_t)(2 * kBufCols + half * (TG_N / 2));
       const uint32_t lcol = hcol + (uint32_t)TG_N;
       float vmax = 0.f;
+      bool oob = false;
       for (int g = 0; g < G; ++g, ++gg) {
         if (!bar_wait(&acc_full[gg & 1], (uint32_t)((gg >> 1) & 1), abrt, 64)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -495,8 +548,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
               const float v = vh + vl;
               const int64_t n = n0 + c0 + i;
               if (mok && n < N) {
-                reinterpret_cast<float*>(out.p)[base + n * out.cs] = v;
-                vmax = fmaxf(vmax, fabsf(v));
+                const int64_t off = base + n * out.cs;
+                if ((uint64_t)off < (uint64_t)out.limit) {
+                  reinterpret_cast<float*>(out.p)[off] = v;
+                  vmax = fmaxf(vmax, fabsf(v));
+                } else {
+                  oob = true;
+                }
               }
             } else {
               if constexpr (MODE == TG_SQSUM_F64) {      // w (vh + vl)^2 to double-FP32
@@ -531,9 +589,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
               for (int i = 0; i < 8; ++i) {
                 const int64_t n = n0 + c0 + i;
                 if (mok && n < N) {
-                  const double v = (double)hi[i] + (double)lo[i];
-                  double* o = C + base + n * out.cs;
-                  *o = out.accumulate ? *o + v : v;
+                  const int64_t off = base + n * out.cs;
+                  if ((uint64_t)off < (uint64_t)out.limit) {
+                    const double v = (double)hi[i] + (double)lo[i];
+                    double* o = C + off;
+                    *o = out.accumulate ? *o + v : v;
+                  } else {
+                    oob = true;
+                  }
                 }
               }
             } else {
@@ -547,6 +610,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
         __syncwarp();
         if (lane == 0) bar_arrive(&acc_empty[gg & 1]);
       }
+      if (oob) atomicExch(err, 2);
       if (!ok) break;
       if constexpr (MODE == TG_STORE_F32) {
         if (out.omax) {
@@ -616,8 +680,16 @@ ttg_status launch_mode(int grid, cudaStream_t st, const CUtensorMap& ma, const C
   k_tgemm<MODE><<<grid, kThreads, kSmem, st>>>(ma, mb, a3 ? 1 : 0, b3 ? 1 : 0, A.amax, B.amax,
                                                (int)A.rows, (int)B.rows, Z, G, kg, sch, out, err);
   TTG_COUNT();
-  const cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? TTG_OK : TTG_CUDA_ERR;
+  cudaError_t e = cudaGetLastError();
+  // TTG_SYNC_LAUNCHES=1: wait for each contraction and report its own error
+  // (debugging: a fault is then charged to the launch that caused it)
+  if (e == cudaSuccess && sync_launches()) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "ttg: k_tgemm<%d> (grid %d, M %lld, N %lld, Z %d, G %d, kg %d) failed: %s\n",
+            MODE, grid, (long long)A.rows, (long long)B.rows, Z, G, kg, cudaGetErrorString(e));
+    return TTG_CUDA_ERR;
+  }
+  return TTG_OK;
 }
 
 // amax[g] = max |x[r][k]| over rows r < rows and k in [g gk, (g+1) gk) within kext
@@ -639,7 +711,8 @@ __global__ void k_group_max(const float* __restrict__ x, int64_t rows, int64_t k
 
 ttg_status tgemm(cudaStream_t st, int mode, const TOperand& A, const TOperand& B, int Z, int G,
                  int kg, const TOut& out, int* err) {
-  if (Z <= 0 || G <= 0 || kg <= 0 || kg * TG_K > 192 || !out.p || !err || out.r1 <= 0)
+  if (Z <= 0 || G <= 0 || kg <= 0 || kg * TG_K > 192 || !out.p || !err || out.r1 <= 0 ||
+      out.limit <= 0)
     return TTG_BAD_ARG;
   if (mode == TG_STORE_F32 && G != 1) return TTG_BAD_ARG;
   if (mode == TG_SQSUM_F64 && (Z != 1 || A.batch < G || !out.w)) return TTG_BAD_ARG;
@@ -691,9 +764,10 @@ extern "C" ttg_status ttg_tc_gemm(int64_t m, int64_t n, int64_t k, const float* 
   TOperand A{a_dev, m, k, lda, 0, 0, am.as<float>()};
   TOperand B{b_dev, n, k, ldb, 0, 0, am.as<float>() + groups};
   TOut o{c_dev, m + 1, ldc, 0, 1, 0};
+  o.limit = (m - 1) * ldc + n;
   TTG_TRY(tgemm(st, TG_SUM_F64, A, B, 1, groups, kg, o, err.as<int>()));
   int e = 0;
   TTG_CUDA_TRY(cudaMemcpyAsync(&e, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   TTG_CUDA_TRY(cudaStreamSynchronize(st));
-  return e ? TTG_TIMEOUT : TTG_OK;
+  return e == 0 ? TTG_OK : e == 2 ? TTG_BAD_ARG : e == 3 ? TTG_CUDA_ERR : TTG_TIMEOUT;
 }

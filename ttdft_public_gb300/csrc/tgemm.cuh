@@ -30,6 +30,8 @@ struct TOut {
   const float* w = nullptr;   // TG_SQSUM_F64: weight of each group
   int accumulate = 0;         // FP64 outputs: add to C instead of overwriting it
   float* omax = nullptr;      // TG_STORE_F32: max |C| per batch (atomicMax into zeroed words)
+  int64_t limit = 0;          // elements of C that may be written: a store at an offset
+                              // outside [0, limit) is skipped and sets err to 2
 };
 
 enum TgemmMode {
@@ -42,8 +44,9 @@ enum TgemmMode {
 // C(m, n, z) = sum_{g < G} sum_{k in group g} A(m, k, z) B(n, k, z) with
 // m < A.rows, n < B.rows, z < Z.  Group g covers K-chunks [g kg, (g+1) kg) of
 // 16 values (TG_SQSUM_F64: every group covers chunks [0, kg) of A's batch g),
-// at most 192 values per group.  `err` is a device int set when a bounded
-// wait ran out.
+// at most 192 values per group.  `err` is a device int set to 1 when a
+// bounded wait ran out, to 2 when a store fell outside out.limit, to 3 when
+// a copy barrier was found out of phase (the kernel stops issuing work).
 ttg_status tgemm(cudaStream_t st, int mode, const TOperand& A, const TOperand& B, int Z, int G,
                  int kg, const TOut& out, int* err);
 

@@ -5,6 +5,7 @@
 #include <cuda_bf16.h>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include <atomic>
@@ -31,11 +32,15 @@
 // (ttg_kernel_launches); TTG_LAUNCHED also counts per operator.
 #define TTG_COUNT() (::ttg::g_kernel_launches.fetch_add(1, std::memory_order_relaxed))
 
-// Checks the last launch; counts it.
+// Checks the last launch; counts it.  With TTG_SYNC_LAUNCHES set in the
+// environment it also waits for the kernel, so that a fault is reported at
+// the launch that caused it (debugging only: it serialises the host).
 #define TTG_LAUNCHED(op)                                                    \
   do {                                                                      \
     (op)->launches++;                                                       \
     cudaError_t e_ = cudaGetLastError();                                    \
+    if (e_ == cudaSuccess && ::ttg::sync_launches())                        \
+      e_ = cudaDeviceSynchronize();                                         \
     if (e_ != cudaSuccess) {                                                \
       fprintf(stderr, "ttg: launch failed: %s (%s:%d)\n",                   \
               cudaGetErrorString(e_), __FILE__, __LINE__);                  \
@@ -45,6 +50,11 @@
 
 namespace ttg {
 extern std::atomic<long long> g_kernel_launches;
+
+inline bool sync_launches() {
+  static const bool on = getenv("TTG_SYNC_LAUNCHES") != nullptr;
+  return on;
+}
 
 constexpr int kGroupRows = 8;       // rows per row group of the SpMM format
 constexpr int kMaxSlots = 16;
