@@ -405,8 +405,9 @@ ttg_status ttg_tc_gemm(int64_t m, int64_t n, int64_t k, const float* a_dev, int6
  *       = 1/2 sum_t omega_t <G, G x1 Kx_t x2 Ky_t x3 Kz_t>,
  *   Kx_t = (Wx Ux)^T E_t (Wx Ux),  E_t[q, q'] = exp(-alpha_t (xq_q - xq_q')^2),
  * the quadrature of the term 1/2 int rho V_H(rho) of the total energy
- * (main.cc:1315-1401 with V_H from dft/KSDFTPotential.cc:269-340), in FP64
- * and exact to rounding without forming V_H on the grid.  ranks = (rx, ry,
+ * (main.cc:1315-1401 with V_H from dft/KSDFTPotential.cc:269-340), from FP64
+ * data without forming V_H on the grid: three double-FP32 GEMMs per term
+ * (about 2^-47 relative per product) and FP64 dot products.  ranks = (rx, ry,
  * rz), G x fastest, nq[d] quadrature points xq_d with weights wq_d, U_d
  * nq[d] x r[d] column-major; all host memory.  Needs no op. */
 ttg_status ttg_hartree_energy(int32_t K, const double* alpha, const double* omega,

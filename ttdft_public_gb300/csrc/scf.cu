@@ -373,50 +373,23 @@ __global__ void k_gauss_apply(const double* __restrict__ alpha, const double* __
   }
 }
 
-// Slab c' of term t of the Hartree energy:
-//   part[t][c'] = sum_{a',b'} G[a',b',c'] (Kx_t Hs Ky_t)[a',b'],
-//   Hs[a,b] = sum_c G[a,b,c] Kz_t[c,c'].
-// K_d (r_d x r_d per term, column-major, symmetric) in global memory; Hs and
-// Kx Hs in dynamic shared memory (2 r0 r1 doubles).
-__global__ void __launch_bounds__(256) k_hartree_energy_slab(
-    const double* __restrict__ G, int r0, int r1, int r2, const double* __restrict__ Kx,
-    const double* __restrict__ Ky, const double* __restrict__ Kz, double* __restrict__ part) {
-  extern __shared__ double hsm[];
-  double* Hs = hsm;
-  double* Tm = hsm + r0 * r1;
-  __shared__ double red[32];
-  const int cp = blockIdx.x, t = blockIdx.y;
-  const double* kx = Kx + (int64_t)t * r0 * r0;
-  const double* ky = Ky + (int64_t)t * r1 * r1;
-  const double* kz = Kz + (int64_t)t * r2 * r2 + (int64_t)cp * r2;   // column c'
-  const int nab = r0 * r1;
-  for (int e = threadIdx.x; e < nab; e += blockDim.x) {
-    double acc = 0.0;
-    for (int c = 0; c < r2; ++c) acc = fma(G[e + (int64_t)nab * c], kz[c], acc);
-    Hs[e] = acc;
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < nab; e += blockDim.x) {
-    const int ap = e % r0, b = e / r0;
-    double acc = 0.0;
-    for (int a = 0; a < r0; ++a) acc = fma(kx[ap + (int64_t)a * r0], Hs[a + r0 * b], acc);
-    Tm[e] = acc;
-  }
-  __syncthreads();
+// Partial sums of <G, U> for one term: part[blockIdx.x] (deterministic: the
+// host adds the partials in order).
+__global__ void __launch_bounds__(256) k_dot_part(const double* __restrict__ G,
+                                                  const double* __restrict__ U, int64_t n,
+                                                  double* __restrict__ part) {
+  __shared__ double red[8];
   double sum = 0.0;
-  for (int e = threadIdx.x; e < nab; e += blockDim.x) {
-    const int ap = e % r0, bp = e / r0;
-    double acc = 0.0;
-    for (int b = 0; b < r1; ++b) acc = fma(Tm[ap + r0 * b], ky[b + (int64_t)bp * r1], acc);
-    sum = fma(G[e + (int64_t)nab * cp], acc, sum);
-  }
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    sum = fma(G[e], U[e], sum);
   for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
   __syncthreads();
   if (threadIdx.x == 0) {
     double tot = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
-    part[(int64_t)t * r2 + cp] = tot;
+    for (int w = 0; w < 8; ++w) tot += red[w];
+    part[blockIdx.x] = tot;
   }
 }
 
@@ -638,28 +611,40 @@ ttg_status ttg_hartree_energy(int32_t K, const double* alpha, const double* omeg
                   DOp{M[d].as<double>(), 1, q, (int64_t)r[d] * q}, Kd[d].as<double>(), 1, r[d],
                   (int64_t)r[d] * r[d], scratch));
   }
-  // E_t = <G, G x1 Kx_t x2 Ky_t x3 Kz_t>, one CTA per (slab c', term t)
-  TTG_TRY(res.alloc((size_t)K * r[2] * 8));
-  const size_t smem = (size_t)2 * r[0] * r[1] * sizeof(double);
-  if (smem > 200 * 1024) return TTG_BAD_ARG;
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
-  std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(k_hartree_energy_slab,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  });
-  if (attr_err != cudaSuccess) return TTG_CUDA_ERR;
-  k_hartree_energy_slab<<<dim3(r[2], K), 256, smem, S.s>>>(
-      core.as<double>(), r[0], r[1], r[2], Kd[0].as<double>(), Kd[1].as<double>(),
-      Kd[2].as<double>(), res.as<double>()); TTG_COUNT();
-  TTG_CUDA_TRY(cudaGetLastError());
-  std::vector<double> e((size_t)K * r[2]);
+  // E_t = <G, G x1 Kx_t x2 Ky_t x3 Kz_t>, term by term as three GEMMs
+  // (H = G x3 Kz_t, T = Kx_t H, U = T x2 Ky_t, slab by slab) and a dot product
+  const int64_t nab = (int64_t)r[0] * r[1];
+  constexpr int kParts = 256;
+  DevBuf hbuf, tbuf;
+  TTG_TRY(hbuf.alloc((size_t)ncore * 8));
+  TTG_TRY(tbuf.alloc((size_t)ncore * 8));
+  TTG_TRY(res.alloc((size_t)K * kParts * 8));
+  double* H = hbuf.as<double>();
+  double* T = tbuf.as<double>();
+  for (int t = 0; t < K; ++t) {
+    const double* kx = Kd[0].as<double>() + (int64_t)t * r[0] * r[0];
+    const double* ky = Kd[1].as<double>() + (int64_t)t * r[1] * r[1];
+    const double* kz = Kd[2].as<double>() + (int64_t)t * r[2] * r[2];
+    // H[(a, b), c'] = sum_c G[(a, b), c] Kz[c, c']
+    TTG_TRY(dgemm(S.s, (int)nab, r[2], r[2], 1, DOp{core.as<double>(), 1, nab, 0},
+                  DOp{kz, 1, r[2], 0}, H, 1, nab, 0, scratch));
+    // T[a', (b, c')] = sum_a Kx[a', a] H[a, (b, c')]
+    TTG_TRY(dgemm(S.s, r[0], (int)((int64_t)r[1] * r[2]), r[0], 1, DOp{kx, 1, r[0], 0},
+                  DOp{H, 1, r[0], 0}, T, 1, r[0], 0, scratch));
+    // U[a', b', c'] = sum_b T[a', b, c'] Ky[b, b'], one batch per slab c' (into H)
+    TTG_TRY(dgemm(S.s, r[0], r[1], r[1], r[2], DOp{T, 1, r[0], nab}, DOp{ky, 1, r[1], 0}, H, 1,
+                  r[0], nab, scratch));
+    k_dot_part<<<kParts, 256, 0, S.s>>>(core.as<double>(), H, ncore,
+                                        res.as<double>() + (int64_t)t * kParts); TTG_COUNT();
+    TTG_CUDA_TRY(cudaGetLastError());
+  }
+  std::vector<double> e((size_t)K * kParts);
   TTG_CUDA_TRY(cudaMemcpyAsync(e.data(), res.p, e.size() * 8, cudaMemcpyDeviceToHost, S.s));
   TTG_CUDA_TRY(cudaStreamSynchronize(S.s));
   double s = 0.0;
   for (int t = 0; t < K; ++t) {
     double et = 0.0;
-    for (int c = 0; c < r[2]; ++c) et += e[(size_t)t * r[2] + c];
+    for (int c = 0; c < kParts; ++c) et += e[(size_t)t * kParts + c];
     s += omega[t] * et;
   }
   *energy = 0.5 * s;
