@@ -352,6 +352,7 @@ def run_ours(args, rank, world):
             "phases_ms": {k_: round(v, 2) for k_, v in phases.items()},
             "tile_fill": info["tile_fill"],
             "umma_tile_fill": (info["nnz_h"] + info["nnz_c"]) / max(1, 128 * info["umma_slots"]),
+            "shifted_orth_steps": info["shifted_orth"],
             "clocks": ck,
             "cpu_baseline": cpu,
         }

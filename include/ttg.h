@@ -77,6 +77,7 @@ typedef struct {
   double tile_fill;       /* (nnz_h + nnz_c^T) / (64 * tile_slots) */
   int64_t umma_tiles;     /* 128-row tiles of the tcgen05 format (0: none) */
   int64_t umma_slots;     /* merged column slots over those tiles */
+  int64_t shifted_orth;   /* shifted Cholesky-QR steps ttg_chfsi_pass needed so far */
 } ttg_op_info_t;
 
 /* ---- device and operator ------------------------------------------------ */
@@ -237,7 +238,13 @@ ttg_status ttg_lanczos_bounds(ttg_op* op, const double* v0_host, int32_t max_ite
 
 /* One ChFSI pass as main.cc:1047-1115 runs it: filter, Cholesky-QR,
  * Rayleigh-Ritz (eigenvalues to w_host, optional), and, if rotate != 0,
- * the rotation X <- X Q. */
+ * the rotation X <- X Q.  Where the reference's orth would meet a
+ * non-positive pivot (the filter has driven columns of a wide block towards
+ * the same eigenvectors), the pass does not fail: it orthonormalises with
+ * shifted Cholesky-QR steps on the unit-diagonal Gram matrix (shift 1e-8)
+ * followed by two plain ones, which keeps the column span and turns
+ * dependent columns into fresh directions; ttg_op_info counts those steps
+ * (shifted_orth). */
 ttg_status ttg_chfsi_pass(ttg_op* op, ttg_block* X, int32_t m, double a, double b,
                           double a0, ttg_sched sched, int32_t rotate, double* w_host);
 

@@ -273,6 +273,30 @@ def test_chfsi_converges_to_exact_eigenvalues(small_op, small_system, mode):
     assert np.abs(w[:nocc] - exact[:nocc]).max() < 1e-6
 
 
+def test_chfsi_pass_survives_dependent_columns(small_op, small_system):
+    """A block with two equal columns stays rank deficient through the
+    filter, so plain Cholesky-QR meets a zero pivot.  The pass orthonormalises
+    with shifted Cholesky-QR steps instead: the result is orthonormal, keeps
+    the other columns' span, and further passes still converge."""
+    s = small_system
+    k, m = 24, 20
+    v0 = np.random.default_rng(4).uniform(0, 1, s.N)
+    upper, lower = api.EigenSolver(small_op).computeUpperBoundWithLanczos(None, 20, v0=v0)
+    X = np.random.default_rng(5).standard_normal((s.N, k))
+    X[:, 7] = X[:, 3]
+    Xm = api.Mat(small_op, k, X)
+    before = small_op.info()["shifted_orth"]
+    sch = api.sched("fp64")
+    w = api.chfsi_pass(small_op, Xm, m, 0.0, upper, lower, sch, rotate=True)
+    assert small_op.info()["shifted_orth"] > before
+    Q = Xm.get()
+    assert np.abs(Q.T @ Q - np.eye(k)).max() < 1e-12
+    for _ in range(14):
+        w = api.chfsi_pass(small_op, Xm, m, w[-1], upper, w[0], sch, rotate=True)
+    exact = np.linalg.eigvalsh(dense_h(s))[:k]
+    assert np.abs(w[:16] - exact[:16]).max() < 1e-6
+
+
 def test_fermi_matches_oracle(small_op):
     eig = np.sort(np.random.default_rng(9).uniform(-1, 1, 64))
     kT = 3.166811429e-6 * 500.0

@@ -49,7 +49,8 @@ class TtgOpInfo(ctypes.Structure):
                 ("group_rows", c_i32), ("n_groups", c_i64), ("stored_cols", c_i64),
                 ("fill", c_dbl), ("device_bytes", c_i64), ("launches", c_i64),
                 ("n_tiles", c_i64), ("tile_slots", c_i64), ("tile_fill", c_dbl),
-                ("umma_tiles", c_i64), ("umma_slots", c_i64)]
+                ("umma_tiles", c_i64), ("umma_slots", c_i64),
+                ("shifted_orth", c_i64)]
 
 
 class TtgSched(ctypes.Structure):

@@ -266,6 +266,7 @@ ttg_status ttg_op_info(const ttg_op* op, ttg_op_info_t* info) {
                         ? (double)(op->nnz_h + op->nnz_c) / (64.0 * op->tiles.slots)
                         : 0.0;
   info->umma_tiles = op->umma.n_tiles;
+  info->shifted_orth = op->shifted_orth;
   info->umma_slots = op->umma.slots;
   return TTG_OK;
 }
@@ -481,17 +482,58 @@ ttg_status ttg_gram(ttg_op* op, const ttg_block* X, const ttg_block* Y, double* 
   return TTG_OK;
 }
 
-ttg_status ttg_chol_qr(ttg_op* op, ttg_block* X) {
-  TTG_TRY(check_block(op, X));
+namespace {
+
+// One Cholesky-QR step.  shifted: factor D^-1 S D^-1 + 1e-8 I instead of S
+// (D = sqrt(diag S)), which is positive definite whatever the columns' norms
+// and their dependence, and apply X <- X (L^-1 D^-1)^T.  The column span is
+// kept; a singular value sigma of the unit-scaled block becomes
+// sigma / sqrt(sigma^2 + 1e-8): about 1 for sigma >> 1e-4 and sigma * 1e4
+// below, so each shifted step divides a condition number above 1e4 by about
+// 1e4 (shifted Cholesky-QR: Fukaya, Kannan, Nakatsukasa, Yamamoto and
+// Yanagisawa, SIAM J. Sci. Comput. 42 (2020) A477-A503).
+ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
   const int k = X->k;
-  TTG_TRY(gram_tn(op, X->x.as<double>(), X->x.as<double>(), k, op->kk0.as<double>()));
-  TTG_TRY(cholesky_inv(op, op->kk0.as<double>(), op->kk1.as<double>(), k, op->status.as<int>()));
+  double* S = op->kk0.as<double>();
+  double* L = op->kk1.as<double>();
+  double* d = op->kk2.as<double>();
+  TTG_TRY(gram_tn(op, X->x.as<double>(), X->x.as<double>(), k, S));
+  if (shifted) TTG_TRY(unit_scale_shift(op, S, d, k, 1e-8));
+  TTG_TRY(cholesky_inv(op, S, L, k, op->status.as<int>()));
   int st = 0;
   TTG_TRY(read_status(op, &st));
   if (st != 0) return TTG_NOT_SPD;
-  TTG_TRY(gemm_nn_small(op, X->x.as<double>(), op->kk1.as<double>(), op->w64.as<double>(), k, 1));
+  if (shifted) TTG_TRY(scale_cols(op, L, d, k));
+  TTG_TRY(gemm_nn_small(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1));
   std::swap(op->w64.p, X->x.p);
   return TTG_OK;
+}
+
+// Orthonormalisation of a filtered block that must not fail: Cholesky-QR,
+// and when its Gram matrix is not numerically positive definite (a block
+// whose columns the filter has driven towards the same few eigenvectors),
+// shifted steps until a plain Cholesky-QR succeeds, then one more plain step
+// for orthogonality (shifted Cholesky-QR3).  A block with exactly dependent
+// columns comes out with those directions replaced by rounding-level ones,
+// orthonormal to the rest: the next filter pass treats them as new start
+// vectors.
+ttg_status chol_qr_robust(ttg_op* op, ttg_block* X, int* shifted_steps) {
+  *shifted_steps = 0;
+  ttg_status s = chol_qr_step(op, X, false);
+  for (int i = 0; s == TTG_NOT_SPD && i < 4; ++i) {
+    TTG_TRY(chol_qr_step(op, X, true));
+    ++*shifted_steps;
+    s = chol_qr_step(op, X, false);
+    if (s == TTG_OK) s = chol_qr_step(op, X, false);
+  }
+  return s;
+}
+
+}  // namespace
+
+ttg_status ttg_chol_qr(ttg_op* op, ttg_block* X) {
+  TTG_TRY(check_block(op, X));
+  return chol_qr_step(op, X, false);
 }
 
 static ttg_status eig_device(ttg_op* op, int k, double* A, double* V, double* w_dev) {
@@ -607,7 +649,9 @@ ttg_status ttg_chfsi_pass(ttg_op* op, ttg_block* X, int32_t m, double a, double 
                           ttg_sched sched, int32_t rotate, double* w_host) {
   TTG_TRY(ttg_cheb_filter(op, X, m, a, b, a0, sched));
   TTG_TRY(umma_check_error(op));
-  TTG_TRY(ttg_chol_qr(op, X));
+  int shifted = 0;
+  TTG_TRY(chol_qr_robust(op, X, &shifted));
+  op->shifted_orth += shifted;
   return ttg_rayleigh_ritz(op, X, rotate, w_host, nullptr);
 }
 

@@ -661,6 +661,50 @@ ttg_status gemm_nn_small(ttg_op* op, const double* X, const double* Q, double* o
   return TTG_OK;
 }
 
+// d[i] = sqrt(S_ii) (1 where that is not a positive finite number)
+__global__ void k_diag_sqrt(const double* __restrict__ S, int k, double* __restrict__ d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) {
+    const double v = S[i + (int64_t)i * k];
+    d[i] = (v > 0.0 && isfinite(v)) ? sqrt(v) : 1.0;
+  }
+}
+
+// S <- D^-1 S D^-1 + shift I (column-major k x k)
+__global__ void k_unit_scale_shift(double* __restrict__ S, const double* __restrict__ d, int k,
+                                   double shift) {
+  const int64_t n = (int64_t)k * k;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % k), j = (int)(e / k);
+    S[e] = S[e] / (d[i] * d[j]) + (i == j ? shift : 0.0);
+  }
+}
+
+// L[:, j] <- L[:, j] / d[j]
+__global__ void k_scale_cols(double* __restrict__ L, const double* __restrict__ d, int k) {
+  const int64_t n = (int64_t)k * k;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    L[e] /= d[e / k];
+}
+
+ttg_status unit_scale_shift(ttg_op* op, double* S, double* d, int k, double shift) {
+  k_diag_sqrt<<<(k + 255) / 256, 256, 0, op->stream>>>(S, k, d); TTG_COUNT();
+  TTG_LAUNCHED(op);
+  const unsigned g = (unsigned)std::min<int64_t>(((int64_t)k * k + 255) / 256, 4096);
+  k_unit_scale_shift<<<g, 256, 0, op->stream>>>(S, d, k, shift); TTG_COUNT();
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
+ttg_status scale_cols(ttg_op* op, double* L, const double* d, int k) {
+  const unsigned g = (unsigned)std::min<int64_t>(((int64_t)k * k + 255) / 256, 4096);
+  k_scale_cols<<<g, 256, 0, op->stream>>>(L, d, k); TTG_COUNT();
+  TTG_LAUNCHED(op);
+  return TTG_OK;
+}
+
 ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_status) {
   k_cholesky_inv<<<1, 1024, 0, op->stream>>>(S, Linv, k, d_status); TTG_COUNT();
   TTG_LAUNCHED(op);

@@ -236,6 +236,7 @@ struct ttg_op {
                               // tensor-core error word shared with the density
   ttg::DensityWork dw;        // density work buffers (ttg_density_device)
   int64_t launches = 0;
+  int64_t shifted_orth = 0;   // shifted Cholesky-QR steps of ttg_chfsi_pass
   int64_t device_bytes = 0;
 };
 
@@ -330,6 +331,10 @@ ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* 
 ttg_status gemm_nn_small(ttg_op* op, const double* X, const double* Q, double* out, int k,
                          int transQ);
 ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_status);
+// S <- D^-1 S D^-1 + shift I with d = sqrt(diag S) written to d (k doubles)
+ttg_status unit_scale_shift(ttg_op* op, double* S, double* d, int k, double shift);
+// L[:, j] <- L[:, j] / d[j]
+ttg_status scale_cols(ttg_op* op, double* L, const double* d, int k);
 ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* d_status);
 ttg_status sym_topk(ttg_op* op, double* A, int n, int r, double* w, double* U, int* d_status);
 ttg_status colmajor_to_rows(ttg_op* op, const double* src, int64_t ld_src, double* dst,
