@@ -213,9 +213,13 @@ def run_ours(args, rank, world):
 
     # ---- timed SCF iterations (mixed filter)
     g = scf.Scf(s, scf_config("mixed"))
+    g.log = log
     it = g.iterate(max_iter=args.warmup + args.steps, tol=0.0)
     for _ in range(args.warmup):
-        next(it)
+        rec = next(it)
+        log(f"warm-up SCF {rec['iter']}: E/atom {rec['e_atom']:.8f}, {rec['passes']} passes, "
+            f"eigenvalues [{rec['eig_lowest']:.5f}, {rec['eig_top']:.5f}], {rec['s']:.2f} s, "
+            + ", ".join(f"{k} {v:.2f}" for k, v in rec["phases"].items()))
     # every fused filter-degree launch of the timed iterations bracketed by
     # CUDA events on the operator's stream
     g.op.kernel_timing(True)

@@ -498,11 +498,26 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
   double* L = op->kk1.as<double>();
   double* d = op->kk2.as<double>();
   TTG_TRY(gram_tn(op, X->x.as<double>(), X->x.as<double>(), k, S));
-  if (shifted) TTG_TRY(unit_scale_shift(op, S, d, k, 1e-8));
+  if (shifted) {
+    int* bad = op->status.as<int>() + 1;
+    TTG_TRY(unit_scale_shift(op, S, d, k, 1e-8, bad));
+    int nbad = 0;
+    TTG_CUDA_TRY(cudaMemcpyAsync(&nbad, bad, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+    TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
+    if (nbad) {
+      fprintf(stderr, "ttg: Cholesky-QR: %d of %d columns have a zero or non-finite norm\n",
+              nbad, k);
+      return TTG_NONFINITE;
+    }
+  }
   TTG_TRY(cholesky_inv(op, S, L, k, op->status.as<int>()));
   int st = 0;
   TTG_TRY(read_status(op, &st));
-  if (st != 0) return TTG_NOT_SPD;
+  if (st != 0) {
+    if (shifted)
+      fprintf(stderr, "ttg: shifted Cholesky-QR: pivot %d of %d not positive\n", st, k);
+    return TTG_NOT_SPD;
+  }
   if (shifted) TTG_TRY(scale_cols(op, L, d, k));
   TTG_TRY(gemm_nn_small(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1));
   std::swap(op->w64.p, X->x.p);
@@ -520,6 +535,8 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
 ttg_status chol_qr_robust(ttg_op* op, ttg_block* X, int* shifted_steps) {
   *shifted_steps = 0;
   ttg_status s = chol_qr_step(op, X, false);
+  if (s == TTG_NOT_SPD && sync_launches())
+    fprintf(stderr, "ttg: Cholesky-QR of the filtered block: non-positive pivot; shifted steps\n");
   for (int i = 0; s == TTG_NOT_SPD && i < 4; ++i) {
     TTG_TRY(chol_qr_step(op, X, true));
     ++*shifted_steps;

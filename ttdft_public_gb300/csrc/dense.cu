@@ -661,12 +661,16 @@ ttg_status gemm_nn_small(ttg_op* op, const double* X, const double* Q, double* o
   return TTG_OK;
 }
 
-// d[i] = sqrt(S_ii) (1 where that is not a positive finite number)
-__global__ void k_diag_sqrt(const double* __restrict__ S, int k, double* __restrict__ d) {
+// d[i] = sqrt(S_ii) (1 where that is not a positive finite number, counted
+// in *bad)
+__global__ void k_diag_sqrt(const double* __restrict__ S, int k, double* __restrict__ d,
+                            int* __restrict__ bad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < k) {
     const double v = S[i + (int64_t)i * k];
-    d[i] = (v > 0.0 && isfinite(v)) ? sqrt(v) : 1.0;
+    const bool ok = v > 0.0 && isfinite(v);
+    d[i] = ok ? sqrt(v) : 1.0;
+    if (!ok) atomicAdd(bad, 1);
   }
 }
 
@@ -689,8 +693,9 @@ __global__ void k_scale_cols(double* __restrict__ L, const double* __restrict__ 
     L[e] /= d[e / k];
 }
 
-ttg_status unit_scale_shift(ttg_op* op, double* S, double* d, int k, double shift) {
-  k_diag_sqrt<<<(k + 255) / 256, 256, 0, op->stream>>>(S, k, d); TTG_COUNT();
+ttg_status unit_scale_shift(ttg_op* op, double* S, double* d, int k, double shift, int* bad) {
+  TTG_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), op->stream));
+  k_diag_sqrt<<<(k + 255) / 256, 256, 0, op->stream>>>(S, k, d, bad); TTG_COUNT();
   TTG_LAUNCHED(op);
   const unsigned g = (unsigned)std::min<int64_t>(((int64_t)k * k + 255) / 256, 4096);
   k_unit_scale_shift<<<g, 256, 0, op->stream>>>(S, d, k, shift); TTG_COUNT();

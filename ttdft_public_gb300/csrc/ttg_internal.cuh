@@ -331,8 +331,9 @@ ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* 
 ttg_status gemm_nn_small(ttg_op* op, const double* X, const double* Q, double* out, int k,
                          int transQ);
 ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_status);
-// S <- D^-1 S D^-1 + shift I with d = sqrt(diag S) written to d (k doubles)
-ttg_status unit_scale_shift(ttg_op* op, double* S, double* d, int k, double shift);
+// S <- D^-1 S D^-1 + shift I with d = sqrt(diag S) written to d (k doubles);
+// *bad (device int) counts diagonal entries that are not positive and finite
+ttg_status unit_scale_shift(ttg_op* op, double* S, double* d, int k, double shift, int* bad);
 // L[:, j] <- L[:, j] / d[j]
 ttg_status scale_cols(ttg_op* op, double* L, const double* d, int k);
 ttg_status syev_device(ttg_op* op, double* A, double* V, double* w, int k, int* d_status);

@@ -118,6 +118,7 @@ class Scf:
         self.torch = torch
         self.s = sysm
         self.cfg = cfg or ScfConfig()
+        self.log = None        # optional callable taking one progress line
         spec = sysm.spec
         self.k = n_states or spec.n_states
         self.m = degree or spec.degree
@@ -444,6 +445,9 @@ class Scf:
             errs = []
             for _ in range(restarts):
                 n_pass += 1
+                if self.log:
+                    self.log(f"SCF {it} pass {n_pass}: filter on [{lower_unwanted:.6g}, "
+                             f"{upper:.6g}], lowest wanted {lower_wanted:.6g}")
                 w = api.chfsi_pass(self.op, X, m, lower_unwanted, upper, lower_wanted, sch,
                                    rotate=True)
                 lower_wanted, lower_unwanted = w[0], w[-1]
