@@ -76,6 +76,10 @@ __global__ void __launch_bounds__(256) k_gram_tn(const double* __restrict__ X,
 #pragma unroll
         for (int v = 0; v < 4; ++v) f2_fma(acc[u][v], a[u], b[v]);
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) f2_renorm(acc[u][v]);
     __syncthreads();
   }
   double* out = part + (int64_t)blockIdx.z * k * k;
@@ -145,6 +149,10 @@ __global__ void __launch_bounds__(256) k_gemm_nn(const double* __restrict__ X,
 #pragma unroll
         for (int v = 0; v < 4; ++v) f2_fma(acc[u][v], a[u], b[v]);
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) f2_renorm(acc[u][v]);
     __syncthreads();
   }
 #pragma unroll

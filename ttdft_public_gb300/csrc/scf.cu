@@ -99,6 +99,10 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, int splits, 
 #pragma unroll
         for (int v = 0; v < 4; ++v) f2_fma(acc[u][v], a[u], b[v]);
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) f2_renorm(acc[u][v]);
     __syncthreads();
   }
 #pragma unroll

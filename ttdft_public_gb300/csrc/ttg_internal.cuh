@@ -300,11 +300,21 @@ __device__ __forceinline__ F2 to_f2(double x) {
   return F2{h, (float)(x - (double)h)};
 }
 
-// acc += a * b.  The accumulator is left unnormalised (lo is not folded
-// into hi after every step): the loop-carried dependency is then a single
-// FP32 add on hi and one on lo, and the sum is read out as (double)hi +
-// (double)lo.  A 4096-term dot product lands within ~6e-14 of the sum of
-// |terms| (FP32: ~4e-8), in a NumPy restatement of these steps.
+// Folds lo into hi (fast two-sum; |lo| is at most a few ulps of hi).  The
+// GEMM loops call it once per 16 steps of f2_fma: lo otherwise grows with
+// the number of steps, and its own FP32 rounding then dominates the error
+// of long sums (tests/test_df64_algorithm.py measures both).
+__device__ __forceinline__ void f2_renorm(F2& acc) {
+  const float s = acc.h + acc.l;
+  acc.l = acc.l - (s - acc.h);
+  acc.h = s;
+}
+
+// acc += a * b.  The accumulator is left unnormalised between renormalisations
+// (lo is not folded into hi after every step): the loop-carried dependency is
+// then a single FP32 add on hi and one on lo, and the sum is read out as
+// (double)hi + (double)lo.  A 4096-term dot product lands within ~6e-14 of
+// the sum of |terms| (FP32: ~4e-8), in a NumPy restatement of these steps.
 __device__ __forceinline__ void f2_fma(F2& acc, F2 a, F2 b) {
   const float p = a.h * b.h;
   float e = fmaf(a.h, b.h, -p);          // exact: a.h b.h = p + e
