@@ -162,8 +162,8 @@ def make_system():
 
 def scf_config(filt, **kw):
     from ttdft_public_gb300 import scf
-    opts = {"history": MIX_DEPTH, **SCF_SETTINGS.get(WORKLOAD, {}), **kw}
-    return scf.ScfConfig(filter=filt, mix_alpha=MIX_ALPHA, max_iter=MAX_ITER, **opts)
+    opts = {"history": MIX_DEPTH, "mix_alpha": MIX_ALPHA, **SCF_SETTINGS.get(WORKLOAD, {}), **kw}
+    return scf.ScfConfig(filter=filt, max_iter=MAX_ITER, **opts)
 
 
 class Timer:
@@ -248,17 +248,28 @@ def run_ours(args, rank, world):
     n = s.N
     peak, peak_kind = peaks()
     roof = {}
+    # blocks wider than 256 states run as one tcgen05 launch per 256-column
+    # block: the roofline unit is one degree over the whole block
+    blocks = -(-k // 256) if k > 256 else 1
     for kind, vsz in (("umma_fp32", 4), ("tc_fp32", 4), ("umma_bf16", 2), ("tc_bf16", 2)):
         ms, cnt = op.kernel_time(kind)
         if cnt == 0:
             continue
-        per = ms / cnt / 1e3
+        nb = blocks if kind.startswith("umma") else 1
+        per = ms / (cnt / nb) / 1e3          # seconds per degree
         # algorithmic bytes of one degree: H in CSR form at the degree's value
         # width (value + int32 column per nonzero, row pointers), Y read, X read,
         # Ynew written
         bytes_deg = nnz * (vsz + 4) + 4 * (n + 1) + 3 * n * k * vsz
-        roof[kind] = {"launch_ms": per * 1e3, "launches": cnt, "bytes_per_launch": bytes_deg,
-                      "flops_per_launch": 2.0 * nnz * k, "achieved": bytes_deg / per / 1e9}
+        roof[kind] = {"launch_ms": ms / cnt, "launches": cnt, "launches_per_degree": nb,
+                      "degree_ms": per * 1e3, "bytes_per_degree": bytes_deg,
+                      "flops_per_degree": 2.0 * nnz * k, "achieved": bytes_deg / per / 1e9}
+    stages = {}
+    for kind in ("orth_gram", "orth_chol", "orth_update", "rr_hx", "rr_gram", "rr_eig",
+                 "rr_rotate", "hartree", "density"):
+        ms, cnt = op.kernel_time(kind)
+        if cnt:
+            stages[kind] = round(ms / args.steps, 2)
     op.kernel_timing(False)
     it.close()
     rho_host = g.rho.cpu().numpy() if rank == 0 else None
@@ -318,7 +329,8 @@ def run_ours(args, rank, world):
             "data": "synthetic (seeded atoms)",
             "config": {"workload": f"{WORKLOAD}: full SCF iteration (mixed filter)",
                        "N": n, "states": k, "degree": m, "bf16_degrees": m // 4,
-                       "quad_points": int(nq), "anderson_depth": MIX_DEPTH, "mix_alpha": MIX_ALPHA,
+                       "quad_points": int(nq), "anderson_depth": g.cfg.history,
+                       "mix_alpha": g.cfg.mix_alpha,
                        "nnz_per_row": info["nnz_h"] / n, "nproj": s.C.n_rows,
                        "passes_per_iter": passes, "iters_timed": [r["iter"] for r in recs],
                        "l2": "inputs larger than L2: H %.2f GB on the device, %d^3 FP64 "
@@ -331,19 +343,24 @@ def run_ours(args, rank, world):
                          "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s",
                          "frac": r32["achieved"] / peak,
                          "traffic": (TRAFFIC_PER_SLOT_UMMA * info["umma_slots"]
-                                     if "umma_fp32" in roof else None),
-                         "traffic_note": "ncu DRAM bytes per 128-row slot of one k_cheb_umma "
-                                         "launch on this workload x this operator's slots",
+                                     if "umma_fp32" in roof and k <= 256 else None),
+                         "traffic_note": ("ncu DRAM bytes per 128-row slot of one k_cheb_umma "
+                                          "launch (160 states) x this operator's slots"
+                                          if k <= 256 else "no ncu capture of the 256-column "
+                                          "block launches"),
+                         "unit_of_work": "one filter degree over the whole block",
                          "timing": "CUDA events around every launch of the kernel on the "
                                    "operator's stream during the timed iterations",
                          "launches": r32["launches"],
-                         "bytes_per_launch": r32["bytes_per_launch"],
-                         "flops_per_launch": r32["flops_per_launch"],
-                         "launch_ms": r32["launch_ms"]},
+                         "launches_per_degree": r32["launches_per_degree"],
+                         "bytes_per_degree": r32["bytes_per_degree"],
+                         "flops_per_degree": r32["flops_per_degree"],
+                         "degree_ms": r32["degree_ms"], "launch_ms": r32["launch_ms"]},
             "roofline_bf16_degree": ({"kernel": ("k_cheb_umma<1, bf16> (tcgen05)" if kb == "umma_bf16"
                                                  else "k_cheb_tc<bf16, 5> (mma.sync)"),
                                       "achieved": roof[kb]["achieved"], "unit": "GB/s",
                                       "frac": roof[kb]["achieved"] / peak,
+                                      "degree_ms": roof[kb]["degree_ms"],
                                       "launch_ms": roof[kb]["launch_ms"],
                                       "launches": roof[kb]["launches"]}
                                      if kb else None),
@@ -354,6 +371,7 @@ def run_ours(args, rank, world):
             "gpu_launches": launches,
             "gpu_launches_per_step": launches / args.steps,
             "phases_ms": {k_: round(v, 2) for k_, v in phases.items()},
+            "stage_device_ms": stages,
             "tile_fill": info["tile_fill"],
             "umma_tile_fill": (info["nnz_h"] + info["nnz_c"]) / max(1, 128 * info["umma_slots"]),
             "shifted_orth_steps": info["shifted_orth"],

@@ -128,9 +128,11 @@ ttg_status ttg_op_sync(ttg_op* op);
 ttg_status ttg_op_record(ttg_op* op, int32_t slot);
 ttg_status ttg_op_elapsed_ms(ttg_op* op, int32_t slot0, int32_t slot1, float* ms);
 
-/* Device time of the fused filter-degree kernels (one launch per degree), by
- * kind.  With timing on, each launch of such a kernel is bracketed by two
- * CUDA events on the operator's stream; the pairs are read back in batches
+/* Device time of the fused filter-degree kernels (one launch per degree, or
+ * per 256-column block of wider blocks) and of the other stages of a ChFSI
+ * pass and an SCF iteration, by kind.  With timing on, each such launch (or
+ * stage) is bracketed by two CUDA events on the operator's stream; the pairs
+ * are read back in batches
  * (no host wait per launch).  ttg_op_kernel_time synchronises the stream and
  * returns the total milliseconds and the launch count of one kind since
  * timing was switched on; enable = 0 switches it off and clears the totals. */
@@ -141,7 +143,14 @@ ttg_status ttg_op_elapsed_ms(ttg_op* op, int32_t slot0, int32_t slot1, float* ms
 #define TTG_KT_UMMA_BF16 4   /* tcgen05 BF16 degree */
 #define TTG_KT_HARTREE 5     /* ttg_hartree_device: factors + three tcgen05 contractions */
 #define TTG_KT_DENSITY 6     /* ttg_density_device: mode products + squared sum */
-#define TTG_KT_KINDS 7
+#define TTG_KT_ORTH_GRAM 7   /* ttg_chfsi_pass orthonormalisation: X^T X */
+#define TTG_KT_ORTH_CHOL 8   /*   Cholesky and L^-1 (k x k) */
+#define TTG_KT_ORTH_UPDATE 9 /*   X <- X L^-T */
+#define TTG_KT_RR_HX 10      /* Rayleigh-Ritz: H X */
+#define TTG_KT_RR_GRAM 11    /*   X^T (H X) */
+#define TTG_KT_RR_EIG 12     /*   k x k eigensolve */
+#define TTG_KT_RR_ROTATE 13  /*   X <- X Q */
+#define TTG_KT_KINDS 14
 ttg_status ttg_op_kernel_timing(ttg_op* op, int32_t enable);
 ttg_status ttg_op_kernel_time(ttg_op* op, int32_t kind, double* ms_total, int64_t* launches);
 

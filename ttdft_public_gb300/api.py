@@ -114,7 +114,8 @@ class Operator:
 
     # kinds of ttg_op_kernel_time (include/ttg.h TTG_KT_*)
     KERNEL_KINDS = {"umma_fp32": 0, "tc_fp32": 1, "tc_bf16": 2, "rowgroup": 3, "umma_bf16": 4,
-                    "hartree": 5, "density": 6}
+                    "hartree": 5, "density": 6, "orth_gram": 7, "orth_chol": 8,
+                    "orth_update": 9, "rr_hx": 10, "rr_gram": 11, "rr_eig": 12, "rr_rotate": 13}
 
     def kernel_timing(self, enable: bool):
         """Bracket every fused filter-degree launch with CUDA events on the

@@ -497,7 +497,9 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
   double* S = op->kk0.as<double>();
   double* L = op->kk1.as<double>();
   double* d = op->kk2.as<double>();
+  TTG_TRY(kt_begin(op, TTG_KT_ORTH_GRAM));
   TTG_TRY(gram_tn(op, X->x.as<double>(), X->x.as<double>(), k, S));
+  TTG_TRY(kt_end(op));
   if (shifted) {
     int* bad = op->status.as<int>() + 1;
     TTG_TRY(unit_scale_shift(op, S, d, k, 1e-8, bad));
@@ -510,7 +512,9 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
       return TTG_NONFINITE;
     }
   }
+  TTG_TRY(kt_begin(op, TTG_KT_ORTH_CHOL));
   TTG_TRY(cholesky_inv(op, S, L, k, op->status.as<int>()));
+  TTG_TRY(kt_end(op));
   int st = 0;
   TTG_TRY(read_status(op, &st));
   if (st != 0) {
@@ -519,7 +523,9 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
     return TTG_NOT_SPD;
   }
   if (shifted) TTG_TRY(scale_cols(op, L, d, k));
+  TTG_TRY(kt_begin(op, TTG_KT_ORTH_UPDATE));
   TTG_TRY(gemm_nn_small(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1));
+  TTG_TRY(kt_end(op));
   std::swap(op->w64.p, X->x.p);
   return TTG_OK;
 }
@@ -585,16 +591,24 @@ ttg_status ttg_rayleigh_ritz(ttg_op* op, ttg_block* X, int32_t rotate, double* w
   TTG_TRY(check_block(op, X));
   const int k = X->k;
   // HX into w64 (FP64 values), then P = X^T HX
+  TTG_TRY(kt_begin(op, TTG_KT_RR_HX));
   TTG_TRY(launch_proj_w(op, TTG_PREC_FP64, X->x.p, k));
   if (op->rr_prec == TTG_PREC_DF64)
     TTG_TRY(launch_apply_df64(op, X->x.as<double>(), op->w64.as<double>(), k));
   else
     TTG_TRY(launch_cheb_step(op, TTG_PREC_FP64, X->x.p, nullptr, op->w64.p, k, 1.0, 0.0, 0.0));
+  TTG_TRY(kt_end(op));
+  TTG_TRY(kt_begin(op, TTG_KT_RR_GRAM));
   TTG_TRY(gram_tn(op, X->x.as<double>(), op->w64.as<double>(), k, op->kk0.as<double>()));
+  TTG_TRY(kt_end(op));
   double* wdev = op->scal.as<double>() + kScalEig;
+  TTG_TRY(kt_begin(op, TTG_KT_RR_EIG));
   TTG_TRY(eig_device(op, k, op->kk0.as<double>(), op->kk1.as<double>(), wdev));
+  TTG_TRY(kt_end(op));
   if (rotate) {
+    TTG_TRY(kt_begin(op, TTG_KT_RR_ROTATE));
     TTG_TRY(gemm_nn_small(op, X->x.as<double>(), op->kk1.as<double>(), op->w64.as<double>(), k, 0));
+    TTG_TRY(kt_end(op));
     std::swap(op->w64.p, X->x.p);
   }
   if (w_host)
