@@ -498,7 +498,7 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
   double* L = op->kk1.as<double>();
   double* d = op->kk2.as<double>();
   TTG_TRY(kt_begin(op, TTG_KT_ORTH_GRAM));
-  TTG_TRY(gram_tn(op, X->x.as<double>(), X->x.as<double>(), k, S));
+  TTG_TRY(gram_tn(op, X->x.as<double>(), X->x.as<double>(), k, S, true));
   TTG_TRY(kt_end(op));
   if (shifted) {
     int* bad = op->status.as<int>() + 1;
@@ -524,7 +524,7 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
   }
   if (shifted) TTG_TRY(scale_cols(op, L, d, k));
   TTG_TRY(kt_begin(op, TTG_KT_ORTH_UPDATE));
-  TTG_TRY(gemm_nn_small(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1));
+  TTG_TRY(gemm_nn_small(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1, true));
   TTG_TRY(kt_end(op));
   std::swap(op->w64.p, X->x.p);
   return TTG_OK;
@@ -599,7 +599,7 @@ ttg_status ttg_rayleigh_ritz(ttg_op* op, ttg_block* X, int32_t rotate, double* w
     TTG_TRY(launch_cheb_step(op, TTG_PREC_FP64, X->x.p, nullptr, op->w64.p, k, 1.0, 0.0, 0.0));
   TTG_TRY(kt_end(op));
   TTG_TRY(kt_begin(op, TTG_KT_RR_GRAM));
-  TTG_TRY(gram_tn(op, X->x.as<double>(), op->w64.as<double>(), k, op->kk0.as<double>()));
+  TTG_TRY(gram_tn(op, X->x.as<double>(), op->w64.as<double>(), k, op->kk0.as<double>(), true));
   TTG_TRY(kt_end(op));
   double* wdev = op->scal.as<double>() + kScalEig;
   TTG_TRY(kt_begin(op, TTG_KT_RR_EIG));

@@ -36,13 +36,24 @@ namespace {
 constexpr int TM = 64, TN = 64, TK = 16;
 
 // S_partial[z] = X[rows_z]^T Y[rows_z]; 256 threads, 4x4 outputs each.
+// sym: blockIdx.x enumerates the tiles on and below the diagonal (tile row
+// pt >= tile column qt, row-major over the triangle), blockIdx.y is 0; the
+// other tiles are not computed (k_reduce_splits mirrors them).
 __global__ void __launch_bounds__(256) k_gram_tn(const double* __restrict__ X,
                                                  const double* __restrict__ Y, int64_t n,
                                                  int k, int64_t ld, int64_t rows_per_split,
-                                                 double* __restrict__ part) {
+                                                 double* __restrict__ part, int sym) {
   __shared__ float sXh[TK][TM + 1], sXl[TK][TM + 1];
   __shared__ float sYh[TK][TN + 1], sYl[TK][TN + 1];
-  const int p0 = blockIdx.x * TM, q0 = blockIdx.y * TN;
+  int pt = blockIdx.x, qt = blockIdx.y;
+  if (sym) {
+    const int t = blockIdx.x;
+    pt = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+    while (pt * (pt + 1) / 2 > t) --pt;
+    while ((pt + 1) * (pt + 2) / 2 <= t) ++pt;
+    qt = t - pt * (pt + 1) / 2;
+  }
+  const int p0 = pt * TM, q0 = qt * TN;
   const int64_t r0 = (int64_t)blockIdx.z * rows_per_split;
   const int64_t r1 = (n < r0 + rows_per_split ? n : r0 + rows_per_split);
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -93,21 +104,31 @@ __global__ void __launch_bounds__(256) k_gram_tn(const double* __restrict__ X,
     }
 }
 
+// S = sum of the split partials.  sym (k > 0): only tiles with tile row >=
+// tile column were computed; S[p, q] for a tile above the diagonal is read
+// from its mirror [q, p].
 __global__ void k_reduce_splits(const double* __restrict__ part, int nsplit, int64_t kk,
-                                double* __restrict__ S) {
+                                double* __restrict__ S, int sym_k) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < kk;
        i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t src = i;
+    if (sym_k > 0) {
+      const int p = (int)(i % sym_k), q = (int)(i / sym_k);
+      if (p / TM < q / TN) src = q + (int64_t)p * sym_k;
+    }
     double s = 0.0;
-    for (int z = 0; z < nsplit; ++z) s += part[(int64_t)z * kk + i];
+    for (int z = 0; z < nsplit; ++z) s += part[(int64_t)z * kk + src];
     S[i] = s;
   }
 }
 
-// out[i, q] = sum_p X[i, p] * Qop[p, q],  Qop = Q or Q^T (Q column-major k x k)
+// out[i, q] = sum_p X[i, p] * Qop[p, q],  Qop = Q or Q^T (Q column-major k x k).
+// transQ with Q lower triangular (L^-1): Qop[p, q] = 0 for p > q, so the sum
+// for the tile's columns [q0, q0 + TN) stops at q0 + TN.
 __global__ void __launch_bounds__(256) k_gemm_nn(const double* __restrict__ X,
                                                  const double* __restrict__ Q,
                                                  double* __restrict__ out, int64_t n, int k,
-                                                 int64_t ld, int transQ) {
+                                                 int64_t ld, int transQ, int lower) {
   __shared__ float sXh[TM][TK + 1], sXl[TM][TK + 1];
   __shared__ float sQh[TK][TN + 1], sQl[TK][TN + 1];
   const int64_t i0 = (int64_t)blockIdx.x * TM;
@@ -118,7 +139,8 @@ __global__ void __launch_bounds__(256) k_gemm_nn(const double* __restrict__ X,
   for (int u = 0; u < 4; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) acc[u][v] = F2{0.f, 0.f};
-  for (int pb = 0; pb < k; pb += TK) {
+  const int kend = (transQ && lower) ? min(k, q0 + TN) : k;
+  for (int pb = 0; pb < kend; pb += TK) {
     for (int e = threadIdx.x; e < TM * TK; e += 256) {
       const int rr = e / TK, cc = e % TK;
       const int64_t row = i0 + rr;
@@ -642,29 +664,32 @@ __global__ void __launch_bounds__(256) k_fermi(const double* eig, int k, double 
 
 }  // namespace
 
-ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* S) {
+ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* S, bool sym) {
   const int tp = (k + TM - 1) / TM, tq = (k + TN - 1) / TN;
-  const int tiles = tp * tq;
+  const int tiles = sym ? tp * (tp + 1) / 2 : tp * tq;
   int64_t nsplit = (2 * 152 + tiles - 1) / tiles;
   nsplit = std::min<int64_t>(nsplit, (op->n + 255) / 256);
   if (nsplit < 1) nsplit = 1;
   const int64_t need = nsplit * (int64_t)k * k * sizeof(double);
   if ((int64_t)op->partial.bytes < need) TTG_TRY(op->partial.alloc(need));
   const int64_t rows = (op->n + nsplit - 1) / nsplit;
-  k_gram_tn<<<dim3(tp, tq, (unsigned)nsplit), 256, 0, op->stream>>>(X, Y, op->n, k, op->ld, rows,
-                                                                   op->partial.as<double>()); TTG_COUNT();
+  const dim3 grid = sym ? dim3((unsigned)tiles, 1, (unsigned)nsplit)
+                        : dim3((unsigned)tp, (unsigned)tq, (unsigned)nsplit);
+  k_gram_tn<<<grid, 256, 0, op->stream>>>(X, Y, op->n, k, op->ld, rows, op->partial.as<double>(),
+                                          sym ? 1 : 0); TTG_COUNT();
   TTG_LAUNCHED(op);
   const int64_t kk = (int64_t)k * k;
   k_reduce_splits<<<(unsigned)std::min<int64_t>((kk + 255) / 256, 1024), 256, 0, op->stream>>>(
-      op->partial.as<double>(), (int)nsplit, kk, S); TTG_COUNT();
+      op->partial.as<double>(), (int)nsplit, kk, S, sym ? k : 0); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
 
 ttg_status gemm_nn_small(ttg_op* op, const double* X, const double* Q, double* out, int k,
-                         int transQ) {
+                         int transQ, bool lower) {
   dim3 grid((unsigned)((op->n + TM - 1) / TM), (unsigned)((k + TN - 1) / TN));
-  k_gemm_nn<<<grid, 256, 0, op->stream>>>(X, Q, out, op->n, k, op->ld, transQ); TTG_COUNT();
+  k_gemm_nn<<<grid, 256, 0, op->stream>>>(X, Q, out, op->n, k, op->ld, transQ,
+                                          lower ? 1 : 0); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }
@@ -915,11 +940,11 @@ extern "C" ttg_status ttg_gram_noalloc(const double* x_dev, const double* y_dev,
   if (nsplit < 1) nsplit = 1;
   const int64_t rows = (n + nsplit - 1) / nsplit;
   ttg::k_gram_tn<<<dim3(tp, tq, (unsigned)nsplit), 256, 0, st>>>(x_dev, y_dev, n, k, ld, rows,
-                                                                scratch); TTG_COUNT();
+                                                                scratch, 0); TTG_COUNT();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return TTG_CUDA_ERR;
   ttg::k_reduce_splits<<<(unsigned)std::min<int64_t>((kk + 255) / 256, 1024), 256, 0, st>>>(
-      scratch, (int)nsplit, kk, s_dev); TTG_COUNT();
+      scratch, (int)nsplit, kk, s_dev, 0); TTG_COUNT();
   e = cudaGetLastError();
   return e == cudaSuccess ? TTG_OK : TTG_CUDA_ERR;
 }

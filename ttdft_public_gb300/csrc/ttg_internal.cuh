@@ -337,9 +337,15 @@ ttg_status dgemm(cudaStream_t st, int M, int N, int K, int batch, DOp A, DOp B, 
                  int64_t c_rs, int64_t c_cs, int64_t c_bs, DevBuf& scratch, bool sym = false);
 
 // dense.cu
-ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* S);
+// S = X^T Y (k x k, column-major).  sym: S is known to be symmetric (X^T X,
+// or X^T H X with H symmetric): only the tiles on and below the diagonal are
+// computed and the others mirrored.
+ttg_status gram_tn(ttg_op* op, const double* X, const double* Y, int k, double* S,
+                   bool sym = false);
+// out = X Q (transQ = 0) or X Q^T (transQ = 1); lower: Q is lower triangular
+// (with transQ the sum over p stops at the output column)
 ttg_status gemm_nn_small(ttg_op* op, const double* X, const double* Q, double* out, int k,
-                         int transQ);
+                         int transQ, bool lower = false);
 ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_status);
 // S <- D^-1 S D^-1 + shift I with d = sqrt(diag S) written to d (k doubles);
 // *bad (device int) counts diagonal entries that are not positive and finite
