@@ -274,6 +274,8 @@ def run_ours(args, rank, world):
         ms, cnt = op.kernel_time(kind)
         if cnt:
             stages[kind] = round(ms / args.steps, 2)
+    log("device ms per iteration by stage:", stages,
+        {kk: round(v["degree_ms"], 2) for kk, v in roof.items()})
     op.kernel_timing(False)
     it.close()
     rho_host = g.rho.cpu().numpy() if rank == 0 else None
@@ -287,6 +289,7 @@ def run_ours(args, rank, world):
         recs3 = [next(it3) for _ in range(args.steps)]
     e2e = max_over_ranks(te.s, world) / args.steps
     nq = g.nq
+    mix_history, mix_alpha = g.cfg.history, g.cfg.mix_alpha
     p3 = float(np.mean([r["passes"] for r in recs3]))
     it3.close()
     g.close()
@@ -333,8 +336,8 @@ def run_ours(args, rank, world):
             "data": "synthetic (seeded atoms)",
             "config": {"workload": f"{WORKLOAD}: full SCF iteration (mixed filter)",
                        "N": n, "states": k, "degree": m, "bf16_degrees": m // 4,
-                       "quad_points": int(nq), "anderson_depth": g.cfg.history,
-                       "mix_alpha": g.cfg.mix_alpha,
+                       "quad_points": int(nq), "anderson_depth": mix_history,
+                       "mix_alpha": mix_alpha,
                        "nnz_per_row": info["nnz_h"] / n, "nproj": s.C.n_rows,
                        "passes_per_iter": passes, "iters_timed": [r["iter"] for r in recs],
                        "l2": "inputs larger than L2: H %.2f GB on the device, %d^3 FP64 "
