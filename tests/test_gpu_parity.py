@@ -181,6 +181,33 @@ def test_gram_and_cholqr(small_op, small_system):
     assert np.abs(Q.T @ Q - np.eye(40)).max() < 1e-12
 
 
+@pytest.mark.parametrize("k", [200, 329])
+def test_blocked_cholqr_wide_blocks(small_system, k):
+    """Blocks wider than 128 states take the blocked Cholesky (64-column
+    panels on many CTAs, the inverse by block forward substitution): with
+    column norms spread over 1e6 the result matches the oracle's Cholesky-QR,
+    and a dependent column is still reported as NOT_SPD with X untouched."""
+    op = api.Operator(api.ProjectHamiltonianSparse.from_system(small_system), k)
+    try:
+        rng = np.random.default_rng(k)
+        X = rng.standard_normal((small_system.N, k)) * np.geomspace(1.0, 1e-6, k)
+        Xm = api.Mat(op, k, X)
+        api.MultTM().orth(Xm)
+        Q = Xm.get()
+        ref, st = oracle.cholqr(X)
+        assert st == 0
+        assert rel(Q, ref) < 1e-9
+        assert np.abs(Q.T @ Q - np.eye(k)).max() < 1e-10
+        X[:, k - 5] = X[:, 150]
+        Xm = api.Mat(op, k, X)
+        with pytest.raises(TtgError) as e:
+            api.MultTM().orth(Xm)
+        assert e.value.status == "NOT_SPD"
+        assert np.array_equal(Xm.get(), X)
+    finally:
+        op.close()
+
+
 def test_cholqr_not_spd_is_reported_and_x_untouched(small_op, small_system):
     X = np.random.default_rng(5).standard_normal((small_system.N, 8))
     X[:, 6] = X[:, 2]

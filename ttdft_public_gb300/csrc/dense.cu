@@ -743,8 +743,254 @@ ttg_status scale_cols(ttg_op* op, double* L, const double* d, int k) {
   return TTG_OK;
 }
 
+// ---- blocked Cholesky and inverse (k > kCholSmall), FP64 on many CTAs ----
+// A (k x k, column-major, lower triangle used) is factored in place in
+// panels of CB columns: the diagonal block in one CTA's shared memory
+// (k_chol_diag, which also inverts it into Linv's diagonal block), the panel
+// below as A21 inv(L11)^T (k_chol_panel), the trailing lower triangle
+// updated by A22 -= L21 L21^T (k_chol_update).  Linv's blocks below the
+// diagonal then follow by block forward substitution, one CTA per block
+// column and 16-column slice (k_chol_inv_offdiag).  The same relative pivot
+// test as k_cholesky_inv: status[0] = j + 1 when pivot j has lost 12 digits
+// of its original diagonal.
+constexpr int CB = 64;
+constexpr int CBP = CB + 1;                  // padded row of a shared tile
+constexpr int kCholSmall = 128;
+constexpr size_t kTileBytes = (size_t)CB * CBP * sizeof(double);   // 33,280
+
+__global__ void __launch_bounds__(256) k_chol_diag(double* __restrict__ A, int k, int j0, int b,
+                                                   const double* __restrict__ diag0,
+                                                   double* __restrict__ Linv,
+                                                   int* __restrict__ status) {
+  // T: the block; its strict upper triangle then holds inv(L11) transposed
+  // (V[i][j] at T[j][i], i > j), the diagonal of inv(L11) in Vd
+  extern __shared__ double sm[];
+  double* T = sm;
+  __shared__ double Vd[CB];
+  __shared__ int bad;
+  if (status[0] != 0) return;
+  for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+    const int i = e % b, j = e / b;
+    T[i * CBP + j] = i >= j ? A[(j0 + i) + (int64_t)(j0 + j) * k] : 0.0;
+  }
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < b; ++j) {
+    if (threadIdx.x == 0) {
+      const double d = T[j * CBP + j], s0 = diag0[j0 + j];
+      if (!(d > 1e-12 * s0) || !(s0 > 0.0) || !isfinite(d)) bad = j0 + j + 1;
+      else T[j * CBP + j] = sqrt(d);
+    }
+    __syncthreads();
+    if (bad) break;
+    const double piv = T[j * CBP + j];
+    for (int i = j + 1 + threadIdx.x; i < b; i += blockDim.x) T[i * CBP + j] /= piv;
+    __syncthreads();
+    const int m = b - j - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int ii = e % m, ll = e / m;
+      if (ll > ii) continue;
+      T[(j + 1 + ii) * CBP + j + 1 + ll] -= T[(j + 1 + ii) * CBP + j] * T[(j + 1 + ll) * CBP + j];
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (threadIdx.x == 0) status[0] = bad;
+    return;
+  }
+  for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+    const int i = e % b, j = e / b;
+    if (i >= j) A[(j0 + i) + (int64_t)(j0 + j) * k] = T[i * CBP + j];
+  }
+  __syncthreads();
+  // inv(L11) by forward substitution, one thread per column j: reads the
+  // lower triangle (never written here) and its own row j of the upper one
+  if (threadIdx.x < b) {
+    const int j = threadIdx.x;
+    Vd[j] = 1.0 / T[j * CBP + j];
+    for (int i = j + 1; i < b; ++i) {
+      double sacc = -T[i * CBP + j] * Vd[j];
+      for (int p = j + 1; p < i; ++p) sacc -= T[i * CBP + p] * T[j * CBP + p];
+      T[j * CBP + i] = sacc / T[i * CBP + i];
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+    const int i = e % b, j = e / b;
+    Linv[(j0 + i) + (int64_t)(j0 + j) * k] = i > j ? T[j * CBP + i] : (i == j ? Vd[i] : 0.0);
+  }
+}
+
+// L21 = A21 inv(L11)^T for the rows [j0 + b + 64 blockIdx.x, +64)
+__global__ void __launch_bounds__(256) k_chol_panel(double* __restrict__ A, int k, int j0, int b,
+                                                    const double* __restrict__ Linv,
+                                                    const int* __restrict__ status) {
+  extern __shared__ double sm[];
+  double* Vt = sm;               // Vt[t][s] = inv(L11)[t][s]
+  double* R = sm + CB * CBP;     // R[r][s] = A21[r][s]
+  if (status[0] != 0) return;
+  const int r0 = j0 + b + blockIdx.x * CB;
+  const int nr = min(CB, k - r0);
+  for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
+    const int i = e % CB, j = e / CB;
+    Vt[i * CBP + j] = (i < b && j < b) ? Linv[(j0 + i) + (int64_t)(j0 + j) * k] : 0.0;
+    R[i * CBP + j] = (i < nr && j < b) ? A[(r0 + i) + (int64_t)(j0 + j) * k] : 0.0;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nr * b; e += blockDim.x) {
+    const int r = e % nr, t = e / nr;
+    double acc = 0.0;
+    for (int sidx = 0; sidx <= t; ++sidx) acc = fma(R[r * CBP + sidx], Vt[t * CBP + sidx], acc);
+    A[(r0 + r) + (int64_t)(j0 + t) * k] = acc;
+  }
+}
+
+// A22 -= L21 L21^T on the tiles of the trailing lower triangle (64 x 64 each)
+__global__ void __launch_bounds__(256) k_chol_update(double* __restrict__ A, int k, int j0, int b,
+                                                     const int* __restrict__ status) {
+  extern __shared__ double sm[];
+  double* Li = sm;
+  double* Ll = sm + CB * CBP;
+  if (status[0] != 0) return;
+  const int s0 = j0 + b;
+  const int t = blockIdx.x;
+  int bi = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  while (bi * (bi + 1) / 2 > t) --bi;
+  while ((bi + 1) * (bi + 2) / 2 <= t) ++bi;
+  const int bj = t - bi * (bi + 1) / 2;
+  const int i0 = s0 + bi * CB, l0 = s0 + bj * CB;
+  for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
+    const int r = e % CB, c = e / CB;
+    Li[r * CBP + c] = (i0 + r < k && c < b) ? A[(i0 + r) + (int64_t)(j0 + c) * k] : 0.0;
+    Ll[r * CBP + c] = (l0 + r < k && c < b) ? A[(l0 + r) + (int64_t)(j0 + c) * k] : 0.0;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  for (int c = 0; c < b; ++c) {
+    double a[4], bb[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a[u] = Li[(ty + 16 * u) * CBP + c];
+      bb[u] = Ll[(tx + 16 * u) * CBP + c];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], bb[v], acc[u][v]);
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = i0 + ty + 16 * u, l = l0 + tx + 16 * v;
+      if (i < k && l < k && l <= i) A[i + (int64_t)l * k] -= acc[u][v];
+    }
+}
+
+// Linv below the diagonal blocks: for block column J and 16 of its columns
+// (blockIdx.y), X_I = -inv(L_II) sum_{J <= P < I} L_IP X_P for I = J+1, ...,
+// with X_J = inv(L_JJ) (already in Linv).
+__global__ void __launch_bounds__(256) k_chol_inv_offdiag(const double* __restrict__ L, int k,
+                                                          double* __restrict__ Linv,
+                                                          const int* __restrict__ status) {
+  extern __shared__ double sm[];
+  double* Lb = sm;                    // L_IP, then inv(L_II): 64 x 65
+  double* Xp = sm + CB * CBP;         // X_P: 64 rows x 16 columns (stride 17)
+  double* Acc = Xp + CB * 17;         // the sum: 64 x 16 (stride 17)
+  if (status[0] != 0) return;
+  const int nb = (k + CB - 1) / CB;
+  const int J = blockIdx.x, c0 = J * CB + blockIdx.y * 16;
+  if (c0 >= k || c0 >= (J + 1) * CB) return;
+  const int nc = min(16, min(k, (J + 1) * CB) - c0);
+  const int r = threadIdx.x % CB, cq = threadIdx.x / CB;   // row, 4-column quarter
+  for (int I = J + 1; I < nb; ++I) {
+    const int i0 = I * CB, ni = min(CB, k - i0);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int P = J; P < I; ++P) {
+      const int p0 = P * CB, np = min(CB, k - p0);
+      __syncthreads();
+      for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
+        const int a = e % CB, bcol = e / CB;
+        Lb[a * CBP + bcol] = (a < ni && bcol < np) ? L[(i0 + a) + (int64_t)(p0 + bcol) * k] : 0.0;
+      }
+      for (int e = threadIdx.x; e < CB * 16; e += blockDim.x) {
+        const int a = e % CB, cc = e / CB;
+        Xp[a * 17 + cc] = (a < np && cc < nc) ? Linv[(p0 + a) + (int64_t)(c0 + cc) * k] : 0.0;
+      }
+      __syncthreads();
+      for (int q = 0; q < np; ++q) {
+        const double lv = Lb[r * CBP + q];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[u] = fma(lv, Xp[q * 17 + 4 * cq + u], acc[u]);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) Acc[r * 17 + 4 * cq + u] = acc[u];
+    for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
+      const int a = e % CB, bcol = e / CB;
+      Lb[a * CBP + bcol] = (a < ni && bcol < ni) ? Linv[(i0 + a) + (int64_t)(i0 + bcol) * k] : 0.0;
+    }
+    __syncthreads();
+    if (r < ni) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int cc = 4 * cq + u;
+        if (cc >= nc) continue;
+        double x = 0.0;
+        for (int q = 0; q <= r; ++q) x = fma(Lb[r * CBP + q], Acc[q * 17 + cc], x);
+        Linv[(i0 + r) + (int64_t)(c0 + cc) * k] = -x;
+      }
+    }
+  }
+}
+
+__global__ void k_copy_diag(const double* __restrict__ A, int k, double* __restrict__ d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) d[i] = A[i + (int64_t)i * k];
+}
+
 ttg_status cholesky_inv(ttg_op* op, double* S, double* Linv, int k, int* d_status) {
-  k_cholesky_inv<<<1, 1024, 0, op->stream>>>(S, Linv, k, d_status); TTG_COUNT();
+  if (k <= kCholSmall) {
+    k_cholesky_inv<<<1, 1024, 0, op->stream>>>(S, Linv, k, d_status); TTG_COUNT();
+    TTG_LAUNCHED(op);
+    return TTG_OK;
+  }
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
+    const int two = (int)(2 * kTileBytes);
+    const int offd = (int)(kTileBytes + 2 * CB * 17 * sizeof(double));
+    cudaError_t e1 = cudaFuncSetAttribute(k_chol_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, two);
+    cudaError_t e2 = cudaFuncSetAttribute(k_chol_update, cudaFuncAttributeMaxDynamicSharedMemorySize, two);
+    cudaError_t e3 = cudaFuncSetAttribute(k_chol_inv_offdiag,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, offd);
+    attr = e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3;
+  });
+  if (attr != cudaSuccess) return TTG_CUDA_ERR;
+  cudaStream_t st = op->stream;
+  if (op->chol.bytes < (size_t)k * 8) TTG_TRY(op->chol.alloc((size_t)k * 8));
+  double* diag0 = op->chol.as<double>();
+  TTG_CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), st));
+  TTG_CUDA_TRY(cudaMemsetAsync(Linv, 0, (size_t)k * k * 8, st));
+  k_copy_diag<<<(k + 255) / 256, 256, 0, st>>>(S, k, diag0); TTG_COUNT();
+  TTG_LAUNCHED(op);
+  for (int j0 = 0; j0 < k; j0 += CB) {
+    const int b = std::min(CB, k - j0);
+    k_chol_diag<<<1, 256, kTileBytes, st>>>(S, k, j0, b, diag0, Linv, d_status); TTG_COUNT();
+    TTG_LAUNCHED(op);
+    const int m = k - j0 - b;
+    if (m <= 0) break;
+    const int rb = (m + CB - 1) / CB;
+    k_chol_panel<<<rb, 256, 2 * kTileBytes, st>>>(S, k, j0, b, Linv, d_status); TTG_COUNT();
+    TTG_LAUNCHED(op);
+    k_chol_update<<<rb * (rb + 1) / 2, 256, 2 * kTileBytes, st>>>(S, k, j0, b, d_status); TTG_COUNT();
+    TTG_LAUNCHED(op);
+  }
+  const int nb = (k + CB - 1) / CB;
+  k_chol_inv_offdiag<<<dim3(nb, CB / 16), 256,
+                       kTileBytes + 2 * CB * 17 * sizeof(double), st>>>(S, k, Linv, d_status); TTG_COUNT();
   TTG_LAUNCHED(op);
   return TTG_OK;
 }

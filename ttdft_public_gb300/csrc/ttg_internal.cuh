@@ -224,6 +224,7 @@ struct ttg_op {
   int rr_prec = TTG_PREC_DF64;  // arithmetic of the Rayleigh-Ritz product H X
   ttg::DevBuf kk0, kk1, kk2;  // k x k FP64 matrices
   ttg::DevBuf kk3;            // eigensolver scratch (k*k + 6k doubles)
+  ttg::DevBuf chol;           // blocked Cholesky: the diagonal before factorisation
   ttg::DevBuf eigbuf;         // eigensolver refinement (5 k*k doubles)
   ttg::DevBuf eigf;           // FP32 tridiagonalisation scratch
   ttg::DevBuf partial;        // split-K partials for the Gram
