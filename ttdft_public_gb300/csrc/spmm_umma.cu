@@ -642,10 +642,19 @@ ttg_status build_umma_tiles(ttg_op* op, int64_t n, const int64_t* hp, const int3
       tptr[t + 1] = ((int64_t)cols.size() + UK - 1) / UK * UK;
     }
   }
+  // Launch order.  While the gathered rows of one launch (three BF16 planes
+  // of up to 256 states per row) fit in L2, tiles run longest first, so the
+  // short ones fill the tail.  Beyond that they run in their spatial order
+  // (x fastest, then y, then z): the ~152 tiles resident at a time then
+  // cover one slab of the Tucker grid, and the rows their columns gather
+  // (the slab plus the band of H around it) stay in L2 while the slab is
+  // worked on, instead of being fetched from HBM for every tile.
   std::vector<int32_t> order(ntiles);
   for (int64_t t = 0; t < ntiles; ++t) order[t] = (int32_t)t;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int32_t a, int32_t b) { return tptr[a + 1] > tptr[b + 1]; });
+  const int64_t gather_bytes = n * (int64_t)std::min(op->max_k, 256) * 6;
+  if (gather_bytes <= ((int64_t)64 << 20))
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t a, int32_t b) { return tptr[a + 1] > tptr[b + 1]; });
   for (int64_t t = 0; t < ntiles; ++t) tptr[t + 1] += tptr[t];
   const int64_t slots = tptr[ntiles];
   const int64_t nchunk = slots / UK;
