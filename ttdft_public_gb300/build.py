@@ -23,7 +23,8 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["spmm.cu", "spmm_tc.cu", "dense.cu", "capi.cu", "tensor.cu", "scf.cu",
-              "hupdate.cu", "eig.cu", "mlp.cu", "spmm_umma.cu", "tgemm.cu"]
+              "hupdate.cu", "eig.cu", "mlp.cu", "spmm_umma.cu", "tgemm.cu",
+              "ozgemm.cu"]
 CXX_SOURCES = ["host/ChebyShevFilter.cc", "host/Mult.cc", "host/MultTm.cc",
                "host/EigenSolver.cc", "host/petsc_shim.cc"]
 

@@ -44,6 +44,24 @@ ttg_status check_block(const ttg_op* op, const ttg_block* b) {
   return TTG_OK;
 }
 
+// S = X^T Y (k x k, column-major) from FP64 blocks: on the tensor cores
+// (ozgemm.cu) where the operands allow, else the double-FP32 CUDA-core kernel.
+ttg_status gram_fp64(ttg_op* op, const double* X, const double* Y, int k, double* S, bool sym) {
+  const OzOperand A{X, k, op->n, op->ld, true}, B{Y, k, op->n, op->ld, true};
+  if (ozgemm_supported(A, B)) return ozgemm(op, A, B, S, 1, k, sym);
+  return gram_tn(op, X, Y, k, S, sym);
+}
+
+// out = X Q (transQ = 0) or X Q^T (transQ = 1; lower: Q lower triangular),
+// Q column-major k x k; the same choice of kernel as gram_fp64.
+ttg_status product_fp64(ttg_op* op, const double* X, const double* Q, double* out, int k,
+                        int transQ, bool lower) {
+  // B(n = q, k = p) = Qop[p, q]: Q[p + q k] (K-major) or, transposed, Q[q + p k] (MN-major)
+  const OzOperand A{X, op->n, k, op->ld, false}, B{Q, k, k, k, transQ != 0};
+  if (ozgemm_supported(A, B)) return ozgemm(op, A, B, out, op->ld, 1, false, transQ && lower);
+  return gemm_nn_small(op, X, Q, out, k, transQ, lower);
+}
+
 }  // namespace
 
 namespace ttg {
@@ -473,7 +491,7 @@ ttg_status ttg_gram(ttg_op* op, const ttg_block* X, const ttg_block* Y, double* 
   TTG_TRY(check_block(op, Y));
   if (X->k != Y->k) return TTG_BAD_ARG;
   const int k = X->k;
-  TTG_TRY(gram_tn(op, X->x.as<double>(), Y->x.as<double>(), k, op->kk0.as<double>()));
+  TTG_TRY(gram_fp64(op, X->x.as<double>(), Y->x.as<double>(), k, op->kk0.as<double>(), false));
   if (s_host) {
     TTG_CUDA_TRY(cudaMemcpyAsync(s_host, op->kk0.p, (size_t)k * k * 8, cudaMemcpyDeviceToHost,
                                  op->stream));
@@ -498,7 +516,7 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
   double* L = op->kk1.as<double>();
   double* d = op->kk2.as<double>();
   TTG_TRY(kt_begin(op, TTG_KT_ORTH_GRAM));
-  TTG_TRY(gram_tn(op, X->x.as<double>(), X->x.as<double>(), k, S, true));
+  TTG_TRY(gram_fp64(op, X->x.as<double>(), X->x.as<double>(), k, S, true));
   TTG_TRY(kt_end(op));
   if (shifted) {
     int* bad = op->status.as<int>() + 1;
@@ -524,7 +542,7 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
   }
   if (shifted) TTG_TRY(scale_cols(op, L, d, k));
   TTG_TRY(kt_begin(op, TTG_KT_ORTH_UPDATE));
-  TTG_TRY(gemm_nn_small(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1, true));
+  TTG_TRY(product_fp64(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1, true));
   TTG_TRY(kt_end(op));
   std::swap(op->w64.p, X->x.p);
   return TTG_OK;
@@ -599,7 +617,7 @@ ttg_status ttg_rayleigh_ritz(ttg_op* op, ttg_block* X, int32_t rotate, double* w
     TTG_TRY(launch_cheb_step(op, TTG_PREC_FP64, X->x.p, nullptr, op->w64.p, k, 1.0, 0.0, 0.0));
   TTG_TRY(kt_end(op));
   TTG_TRY(kt_begin(op, TTG_KT_RR_GRAM));
-  TTG_TRY(gram_tn(op, X->x.as<double>(), op->w64.as<double>(), k, op->kk0.as<double>(), true));
+  TTG_TRY(gram_fp64(op, X->x.as<double>(), op->w64.as<double>(), k, op->kk0.as<double>(), true));
   TTG_TRY(kt_end(op));
   double* wdev = op->scal.as<double>() + kScalEig;
   TTG_TRY(kt_begin(op, TTG_KT_RR_EIG));
@@ -607,7 +625,8 @@ ttg_status ttg_rayleigh_ritz(ttg_op* op, ttg_block* X, int32_t rotate, double* w
   TTG_TRY(kt_end(op));
   if (rotate) {
     TTG_TRY(kt_begin(op, TTG_KT_RR_ROTATE));
-    TTG_TRY(gemm_nn_small(op, X->x.as<double>(), op->kk1.as<double>(), op->w64.as<double>(), k, 0));
+    TTG_TRY(product_fp64(op, X->x.as<double>(), op->kk1.as<double>(), op->w64.as<double>(), k, 0,
+                         false));
     TTG_TRY(kt_end(op));
     std::swap(op->w64.p, X->x.p);
   }
@@ -626,9 +645,11 @@ ttg_status ttg_rotate(ttg_op* op, ttg_block* X, const double* q_host) {
   const int k = X->k;
   TTG_CUDA_TRY(cudaMemcpyAsync(op->kk1.p, q_host, (size_t)k * k * 8, cudaMemcpyHostToDevice,
                                op->stream));
-  TTG_TRY(gemm_nn_small(op, X->x.as<double>(), op->kk1.as<double>(), op->w64.as<double>(), k, 0));
+  TTG_TRY(product_fp64(op, X->x.as<double>(), op->kk1.as<double>(), op->w64.as<double>(), k, 0,
+                       false));
   std::swap(op->w64.p, X->x.p);
   TTG_CUDA_TRY(cudaStreamSynchronize(op->stream));
+  TTG_TRY(ozgemm_error(op));
   return TTG_OK;
 }
 
@@ -683,7 +704,8 @@ ttg_status ttg_chfsi_pass(ttg_op* op, ttg_block* X, int32_t m, double a, double 
   int shifted = 0;
   TTG_TRY(chol_qr_robust(op, X, &shifted));
   op->shifted_orth += shifted;
-  return ttg_rayleigh_ritz(op, X, rotate, w_host, nullptr);
+  TTG_TRY(ttg_rayleigh_ritz(op, X, rotate, w_host, nullptr));
+  return ozgemm_error(op);
 }
 
 ttg_status ttg_fermi(ttg_op* op, int32_t k, const double* eig_host, double n_electrons, double kT,

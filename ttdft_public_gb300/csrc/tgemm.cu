@@ -62,9 +62,12 @@
 
 #include "ttg_internal.cuh"
 #include "tgemm.cuh"
+#include "tc_common.cuh"
 
 namespace ttg {
 namespace {
+
+using namespace tc;
 
 constexpr int TG_M = 128;                         // rows of an A tile (MMA M)
 constexpr int TG_N = 48;                          // rows of a B tile (MMA N)
@@ -84,22 +87,8 @@ constexpr int kEpiWarp0 = 10, kEpiWarps = 8;      // two warps per 32 TMEM lanes
 constexpr int kThreads = (kEpiWarp0 + kEpiWarps) * 32;   // 576
 constexpr int kBufCols = 4 * TG_N;                // four level accumulators per buffer
 constexpr uint32_t kTmemCols = 512;               // 2 buffers (384) + hi, lo (96)
-constexpr int kMaxWait = 1 << 22;
 
-__device__ __forceinline__ uint32_t su32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
 
-// canonical K-major layout, no swizzle: core matrices of 8 rows x 16 bytes,
-// 128 bytes apart along K (leading byte offset), 256 bytes apart along rows
-// (stride byte offset)
-__device__ __forceinline__ uint64_t kmajor_desc(uint32_t addr) {
-  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFF);
-  d |= (uint64_t)(128 >> 4) << 16;
-  d |= (uint64_t)(256 >> 4) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;
-}
 
 // kind::f16: BF16 x BF16 -> FP32, A and B K-major, M = 128, N = 48
 __device__ __forceinline__ uint32_t idesc_mma() {
@@ -107,74 +96,12 @@ __device__ __forceinline__ uint32_t idesc_mma() {
          ((uint32_t)(TG_M >> 4) << 24);
 }
 
-__device__ __forceinline__ void bar_init(uint64_t* b, int count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count));
-}
 
-__device__ __forceinline__ bool bar_try(uint64_t* b, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(su32(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
 
-// bounded wait; gives up early when another role has aborted
-__device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag,
-                                         int ns) {
-  for (int i = 0; i < kMaxWait; ++i) {
-    if (bar_try(b, parity)) return true;
-    if (*abort_flag) return false;
-    if (ns) __nanosleep(ns);
-  }
-  *abort_flag = 1;
-  return false;
-}
 
-// bounded wait that ignores the abort flag: on the abort path, for copies and
-// MMAs already issued to complete before the CTA releases its memory
-__device__ __forceinline__ bool bar_drain(uint64_t* b, uint32_t parity) {
-  for (int i = 0; i < kMaxWait; ++i) {
-    if (bar_try(b, parity)) return true;
-    __nanosleep(128);
-  }
-  return false;
-}
 
-// non-blocking: has the phase of this parity completed (is the barrier past it)?
-__device__ __forceinline__ bool bar_test(uint64_t* b, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(su32(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
 
-__device__ __forceinline__ void bar_arrive(uint64_t* b) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
-}
 
-__device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap* map, int c0, int c1,
-                                         int c2, bool three_d, uint32_t bar) {
-  if (three_d)
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];"
-        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
-        : "memory");
-  else
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3}], [%4];"
-        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
-        : "memory");
-}
 
 struct TileSched {
   int tiles_m, tiles_n;
@@ -221,26 +148,7 @@ __device__ __forceinline__ void slice8(const float* v, float sc, uint4& p0, uint
   p2 = make_uint4(w2[0], w2[1], w2[2], w2[3]);
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t addr, float* v) {
-  uint32_t r[8];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7])
-      : "r"(addr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
-}
 
-__device__ __forceinline__ void tmem_st8(uint32_t addr, const float* v) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
-      ::"r"(addr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])),
-        "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])),
-        "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
-      : "memory");
-}
 
 }  // namespace
 }  // namespace ttg
@@ -362,7 +270,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
       if (lane == 0) {
         // chunk q has landed (published in order by warp 3)
         w = false;
-        for (int i = 0; i < kMaxWait; ++i) {
+        for (int i = 0; i < kTcMaxWait; ++i) {
           uint32_t l;
           asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(l) : "r"(su32(&landed))
                        : "memory");
@@ -459,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tgemm(
           for (int c = 0; c < kg; ++c, ++q) {
             // polling with a short back-off: spinning threads take issue slots
             // from the converter and epilogue warps
-            for (int i = 0; i < kMaxWait && avail <= (uint32_t)q; ++i) {
+            for (int i = 0; i < kTcMaxWait && avail <= (uint32_t)q; ++i) {
               asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(avail)
                            : "r"(su32(&ready)) : "memory");
               if (avail > (uint32_t)q || *abrt) break;

@@ -225,6 +225,8 @@ struct ttg_op {
   ttg::DevBuf kk0, kk1, kk2;  // k x k FP64 matrices
   ttg::DevBuf kk3;            // eigensolver scratch (k*k + 6k doubles)
   ttg::DevBuf chol;           // blocked Cholesky: the diagonal before factorisation
+  ttg::DevBuf oz_exp;         // FP64 tensor-core GEMM: row scales of its operands
+  ttg::DevBuf oz_err;         // FP64 tensor-core GEMM: error word
   ttg::DevBuf eigbuf;         // eigensolver refinement (5 k*k doubles)
   ttg::DevBuf eigf;           // FP32 tridiagonalisation scratch
   ttg::DevBuf partial;        // split-K partials for the Gram
@@ -336,6 +338,25 @@ struct DOp {
 };
 ttg_status dgemm(cudaStream_t st, int M, int N, int K, int batch, DOp A, DOp B, double* C,
                  int64_t c_rs, int64_t c_cs, int64_t c_bs, DevBuf& scratch, bool sym = false);
+
+// ozgemm.cu: FP64-accurate C = A B^T on the tensor cores (see the file).
+// A FP64 operand: `rows` rows of `kext` values, K-major (element (r, k) at
+// p[r ld + k]) or MN-major (p[k ld + r]); ld * 8 a multiple of 16.
+struct OzOperand {
+  const double* p;
+  int64_t rows, kext, ld;
+  bool mn_major;
+};
+// Whether ozgemm takes these operands (TMA alignment, sizes; off with
+// TTG_DISABLE_OZGEMM); callers fall back to the double-FP32 CUDA-core GEMMs.
+bool ozgemm_supported(const OzOperand& A, const OzOperand& B);
+// C[m c_rs + n c_cs] = sum_k A(m, k) B(n, k).  sym: A B^T is symmetric (A = B,
+// or B = H A): only tiles on and below the diagonal are computed and the
+// others mirrored.  b_lower: B(n, k) = 0 for k > n (the sum stops at n).
+ttg_status ozgemm(ttg_op* op, const OzOperand& A, const OzOperand& B, double* C, int64_t c_rs,
+                  int64_t c_cs, bool sym, bool b_lower = false);
+// Reads and clears the tensor-core GEMM's error word (synchronises).
+ttg_status ozgemm_error(ttg_op* op);
 
 // dense.cu
 // S = X^T Y (k x k, column-major).  sym: S is known to be symmetric (X^T X,
