@@ -76,6 +76,8 @@ def test_rotation_and_orthonormalisation(small_system, k):
         ref, st = oracle.cholqr(X)
         assert st == 0
         assert np.max(np.abs(Qo - ref)) < 1e-10
-        assert np.abs(Qo.T @ Qo - np.eye(k)).max() < 1e-11
+        # one Cholesky-QR of a block of condition ~1e4: orthogonality to
+        # ~cond^2 u (FP64 gives the same order)
+        assert np.abs(Qo.T @ Qo - np.eye(k)).max() < 1e-9
     finally:
         op.close()
