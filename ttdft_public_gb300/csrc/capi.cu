@@ -542,7 +542,10 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
   }
   if (shifted) TTG_TRY(scale_cols(op, L, d, k));
   TTG_TRY(kt_begin(op, TTG_KT_ORTH_UPDATE));
-  TTG_TRY(product_fp64(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1, true));
+  // X L^-T stays on the double-FP32 kernel: L^-T undoes the columns' scales,
+  // which per-row digit scales of X cannot resolve (a column 1e-6 of the
+  // largest would keep only ~28 of its bits)
+  TTG_TRY(gemm_nn_small(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1, true));
   TTG_TRY(kt_end(op));
   std::swap(op->w64.p, X->x.p);
   return TTG_OK;
