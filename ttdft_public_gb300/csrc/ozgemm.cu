@@ -90,36 +90,65 @@ __device__ __forceinline__ uint32_t idesc_oz() {
 // Six balanced base-256 digits of v 2^(8 - e) (see the file comment) from the
 // bits of v; zero for zeros and subnormals (below 2^-1022, far under the
 // 2^-40 resolution of any row whose scale is a normal number); NaN in, NaN out.
+// One 64-bit shift places the 48-bit fixed-point value; the digits come from
+// its two 24-bit halves with 32-bit integer operations.
 __device__ __forceinline__ void digits6(double v, int e, float* d) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-  const int E = (int)((bits >> 52) & 0x7FF);
+  const int hi = __double2hiint(v);
+  const uint32_t lo = (uint32_t)__double2loint(v);
+  const int E = (hi >> 20) & 0x7FF;
   if (E == 0x7FF) {
 #pragma unroll
     for (int i = 0; i < kDigits; ++i) d[i] = __int_as_float(0x7fc00000);
     return;
   }
-  unsigned long long X = 0;
+  uint32_t xl = 0, xh = 0;
   if (E != 0) {
-    const unsigned long long M = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-    // v 2^(8-e) 2^40 = M 2^(E - 1075 + 48 - e); |v| < 2^e makes the shift <= -5
+    const unsigned long long M =
+        ((unsigned long long)((hi & 0xFFFFF) | 0x100000) << 32) | lo;
+    // v 2^(8-e) 2^40 = M 2^(E - 1075 + 48 - e); |v| < 2^e makes the shift >= 5
     const int rs = 1075 - 48 + e - E;
-    if (rs < 63) X = (M + (1ull << (rs - 1))) >> rs;   // rounded to nearest
-  }
-  int t[kDigits];
-#pragma unroll
-  for (int i = kDigits - 1; i >= 1; --i) {
-    int dg = (int)(X & 255ull);
-    X >>= 8;
-    if (dg >= 128) {
-      dg -= 256;
-      X += 1;
+    if (rs < 63) {
+      const unsigned long long X = (M + (1ull << (rs - 1))) >> rs;   // rounded, < 2^48 + 1
+      xl = (uint32_t)X & 0xFFFFFFu;
+      xh = (uint32_t)(X >> 24);
     }
-    t[i] = dg;
   }
-  t[0] = (int)X;                                        // 0 .. 256
-  const float sgn = (bits >> 63) ? -1.f : 1.f;
+  // balanced digits, lowest first: d = ((t + 128) mod 256) - 128, t <- (t + 128) / 256
+  int t = (int)xl, g[kDigits];
+  g[5] = ((t + 128) & 255) - 128; t = (t + 128) >> 8;
+  g[4] = ((t + 128) & 255) - 128; t = (t + 128) >> 8;
+  g[3] = ((t + 128) & 255) - 128; t = (t + 128) >> 8;
+  int u = (int)xh + t;
+  g[2] = ((u + 128) & 255) - 128; u = (u + 128) >> 8;
+  g[1] = ((u + 128) & 255) - 128; u = (u + 128) >> 8;
+  g[0] = u;                                             // 0 .. 256
+  const int sm = hi >> 31;                              // 0 or -1
 #pragma unroll
-  for (int i = 0; i < kDigits; ++i) d[i] = sgn * (float)t[i];
+  for (int i = 0; i < kDigits; ++i) d[i] = (float)((g[i] ^ sm) - sm);
+}
+
+// three 8-column tensor-memory loads and one wait, in one statement (the
+// registers are defined only after the wait)
+__device__ __forceinline__ void tmem_ld8x3(uint32_t a0, uint32_t a1, uint32_t a2, float* v0,
+                                           float* v1, float* v2) {
+  uint32_t r[24];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%24];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%25];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16,%17,%18,%19,%20,%21,%22,%23}, [%26];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23])
+      : "r"(a0), "r"(a1), "r"(a2)
+      : "memory");
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    v0[j] = __uint_as_float(r[j]);
+    v1[j] = __uint_as_float(r[8 + j]);
+    v2[j] = __uint_as_float(r[16 + j]);
+  }
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -287,6 +316,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
       const double* rb = reinterpret_cast<const double*>(raw + s * kRawStage + kRawA);
       unsigned char* dst = spl + s2 * kSplStage;
       // element pairs (row, k, k + 1): 128 x 8 of A, then 32 x 8 of B
+      // (two pairs in flight per lane: the digit arithmetic is a long chain)
+#pragma unroll 2
       for (int p = lane; p < (OZ_M + OZ_N) * 8; p += 32) {
         const bool isb = p >= OZ_M * 8;
         const int pp = isb ? p - OZ_M * 8 : p;
@@ -403,8 +434,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
 #pragma unroll
       for (int c0 = 0; c0 < OZ_N; c0 += 8) {
         float S[kLevels][8];
-#pragma unroll
-        for (int L = 0; L < kLevels; ++L) tmem_ld8(acol + L * OZ_N + c0, S[L]);
+        tmem_ld8x3(acol + c0, acol + OZ_N + c0, acol + 2 * OZ_N + c0, S[0], S[1], S[2]);
+        tmem_ld8x3(acol + 3 * OZ_N + c0, acol + 4 * OZ_N + c0, acol + 5 * OZ_N + c0, S[3], S[4],
+                   S[5]);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           // S0 + S1 2^-8 + ... + S5 2^-40 as (h, l), then into (hi, lo)
