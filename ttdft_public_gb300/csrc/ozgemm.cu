@@ -161,6 +161,38 @@ __device__ __forceinline__ int plane_off(int row, int k) {
   return (row >> 3) * 256 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
+// Digit planes of one chunk of R operand rows (raw FP64 tile, either
+// layout) by one warp.  Lane (r8, kp) = (lane / 4, lane % 4) takes the pair
+// (row 8 rb + r8, k = 8 kh + 2 kp, k + 1): the 32 lanes of one step then
+// store to 32 different banks of each plane (plane_off).  Two steps in
+// flight per lane: the digit arithmetic is a long dependent chain.
+template <int R, int MN>
+__device__ __forceinline__ void slice_rows(const double* __restrict__ raw, const int* es,
+                                           unsigned char* planes, int plane_bytes, int lane) {
+  const int r8 = lane >> 2, kp = lane & 3;
+#pragma unroll 2
+  for (int it = 0; it < R / 4; ++it) {
+    const int row = 8 * (it >> 1) + r8, k = 8 * (it & 1) + 2 * kp;
+    double v0, v1;
+    if (MN) {                 // raw [k][row]
+      v0 = raw[k * R + row];
+      v1 = raw[(k + 1) * R + row];
+    } else {                  // raw [row][16]
+      const double2 vv = *reinterpret_cast<const double2*>(raw + row * OZ_K + k);
+      v0 = vv.x;
+      v1 = vv.y;
+    }
+    const int e = es[row];
+    float d0[kDigits], d1[kDigits];
+    digits6(v0, e, d0);
+    digits6(v1, e, d1);
+    const int off = plane_off(row, k);
+#pragma unroll
+    for (int d = 0; d < kDigits; ++d)
+      *reinterpret_cast<uint32_t*>(planes + d * plane_bytes + off) = pack_bf16(d0[d], d1[d]);
+  }
+}
+
 struct OzTiles {
   int tiles_m, tiles_n;
   int sym;          // only tiles with n0 <= m0 + 127 (on and below the diagonal)
@@ -315,39 +347,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
       const double* ra = reinterpret_cast<const double*>(raw + s * kRawStage);
       const double* rb = reinterpret_cast<const double*>(raw + s * kRawStage + kRawA);
       unsigned char* dst = spl + s2 * kSplStage;
-      // element pairs (row, k, k + 1): 128 x 8 of A, then 32 x 8 of B
-      // (two pairs in flight per lane: the digit arithmetic is a long chain)
-#pragma unroll 2
-      for (int p = lane; p < (OZ_M + OZ_N) * 8; p += 32) {
-        const bool isb = p >= OZ_M * 8;
-        const int pp = isb ? p - OZ_M * 8 : p;
-        const int R = isb ? OZ_N : OZ_M;
-        int row, k;
-        double v0, v1;
-        if (isb ? B_MN : A_MN) {          // raw [k][row]: consecutive lanes, consecutive rows
-          row = pp % R;
-          k = 2 * (pp / R);
-          const double* r_ = isb ? rb : ra;
-          v0 = r_[k * R + row];
-          v1 = r_[(k + 1) * R + row];
-        } else {                          // raw [row][16]: consecutive lanes, consecutive k
-          row = pp >> 3;
-          k = 2 * (pp & 7);
-          const double2 vv = *reinterpret_cast<const double2*>((isb ? rb : ra) + row * OZ_K + k);
-          v0 = vv.x;
-          v1 = vv.y;
-        }
-        const int e = isb ? eB[row] : eA[row];
-        float d0[kDigits], d1[kDigits];
-        digits6(v0, e, d0);
-        digits6(v1, e, d1);
-        const int off = plane_off(row, k);
-        unsigned char* base = dst + (isb ? kDigits * kPlA : 0);
-        const int pl = isb ? kPlB : kPlA;
-#pragma unroll
-        for (int d = 0; d < kDigits; ++d)
-          *reinterpret_cast<uint32_t*>(base + d * pl + off) = pack_bf16(d0[d], d1[d]);
-      }
+      slice_rows<OZ_M, A_MN>(ra, eA, dst, kPlA, lane);
+      slice_rows<OZ_N, B_MN>(rb, eB, dst + kDigits * kPlA, kPlB, lane);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) {
