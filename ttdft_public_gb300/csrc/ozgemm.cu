@@ -29,11 +29,10 @@
 //  - warp 0, one thread: TMA tile loads of the FP64 operands (box 16 x 128 of
 //    A, 16 x 32 of B, either layout) into a raw ring of 3 stages;
 //  - warp 3, one thread: waits for the raw copies in order and publishes the
-//    count of landed chunks (the slicing warps take chunks round-robin and
-//    cannot use parity waits on the raw barriers themselves);
-//  - warps 4-8, whole chunks in turn: cut the 160 rows x 16 values of a chunk
-//    into six digit planes each, in the canonical K-major MMA layout, into a
-//    ring of 5 stages;
+//    count of landed chunks (one thread polls the barriers, not five warps);
+//  - warps 4-8, each a fifth of the rows of every chunk: cut the 160 rows x
+//    16 values into six digit planes each, in the canonical K-major MMA
+//    layout, into a ring of 5 stages;
 //  - warp 2, one thread: waits for the digit planes (and, before a group, for
 //    the epilogue to have emptied the accumulator buffer it will use) and
 //    publishes the count of ready chunks;
@@ -75,7 +74,7 @@ constexpr int kSplStage = kDigits * (kPlA + kPlB);      // 30 KB
 constexpr int kRawStages = 3;
 constexpr int kSplStages = 5;
 constexpr int kSmem = kRawStages * kRawStage + kSplStages * kSplStage + 1024;
-constexpr int kConvWarp0 = 4, kConvWarps = 5;           // <= kSplStages: one-phase waits
+constexpr int kConvWarp0 = 4, kConvWarps = 5;           // share every chunk's rows
 constexpr int kEpiWarp0 = 9, kEpiWarps = 4;
 constexpr int kThreads = (kEpiWarp0 + kEpiWarps) * 32;  // 416
 constexpr int kBufCols = kLevels * OZ_N;                // 192
@@ -161,31 +160,35 @@ __device__ __forceinline__ int plane_off(int row, int k) {
   return (row >> 3) * 256 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
-// Digit planes of one chunk of R operand rows (raw FP64 tile, either
-// layout) by one warp.  Lane (r8, kp) = (lane / 4, lane % 4) takes the pair
-// (row 8 rb + r8, k = 8 kh + 2 kp, k + 1): the 32 lanes of one step then
-// store to 32 different banks of each plane (plane_off).  Two steps in
-// flight per lane: the digit arithmetic is a long dependent chain.
+// Digit planes of one block of 8 operand rows of a chunk (raw FP64 tile of
+// R rows, either layout) by one warp.  Lane (r8, kp) = (lane / 4, lane % 4)
+// takes the pairs (row 8 rb + r8, k = 8 kh + 2 kp, k + 1), kh = 0, 1: the 32
+// lanes of a step store to 32 different banks of each plane (plane_off).
 template <int R, int MN>
-__device__ __forceinline__ void slice_rows(const double* __restrict__ raw, const int* es,
-                                           unsigned char* planes, int plane_bytes, int lane) {
-  const int r8 = lane >> 2, kp = lane & 3;
-#pragma unroll 2
-  for (int it = 0; it < R / 4; ++it) {
-    const int row = 8 * (it >> 1) + r8, k = 8 * (it & 1) + 2 * kp;
-    double v0, v1;
+__device__ __forceinline__ void slice_block(const double* __restrict__ raw, const int* es,
+                                            unsigned char* planes, int plane_bytes, int rb,
+                                            int lane) {
+  const int row = 8 * rb + (lane >> 2), kp = lane & 3;
+  const int e = es[row];
+  double v[2][2];
+#pragma unroll
+  for (int kh = 0; kh < 2; ++kh) {
+    const int k = 8 * kh + 2 * kp;
     if (MN) {                 // raw [k][row]
-      v0 = raw[k * R + row];
-      v1 = raw[(k + 1) * R + row];
+      v[kh][0] = raw[k * R + row];
+      v[kh][1] = raw[(k + 1) * R + row];
     } else {                  // raw [row][16]
       const double2 vv = *reinterpret_cast<const double2*>(raw + row * OZ_K + k);
-      v0 = vv.x;
-      v1 = vv.y;
+      v[kh][0] = vv.x;
+      v[kh][1] = vv.y;
     }
-    const int e = es[row];
+  }
+#pragma unroll
+  for (int kh = 0; kh < 2; ++kh) {
+    const int k = 8 * kh + 2 * kp;
     float d0[kDigits], d1[kDigits];
-    digits6(v0, e, d0);
-    digits6(v1, e, d1);
+    digits6(v[kh][0], e, d0);
+    digits6(v[kh][1], e, d1);
     const int off = plane_off(row, k);
 #pragma unroll
     for (int d = 0; d < kDigits; ++d)
@@ -249,10 +252,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
   if (tid == 32) {
     for (int s = 0; s < kRawStages; ++s) {
       bar_init(&raw_full[s], 1);
-      bar_init(&raw_empty[s], 1);
+      bar_init(&raw_empty[s], kConvWarps);
     }
     for (int s = 0; s < kSplStages; ++s) {
-      bar_init(&spl_full[s], 1);
+      bar_init(&spl_full[s], kConvWarps);
       bar_init(&spl_empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -323,9 +326,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
       }
     }
   } else if (warp >= kConvWarp0 && warp < kConvWarp0 + kConvWarps) {
-    // ---- digit planes, chunk q to converter warp q % kConvWarps
+    // ---- digit planes: every converter warp takes its share of the rows of
+    // every chunk (row blocks of 8: cw, cw + 5, ...), so a chunk's raw stage
+    // is released after a fifth of the work; each warp waits on every phase
+    // of the barriers it uses, in order
     const int cw = warp - kConvWarp0;
-    for (int q = cw; q < nq; q += kConvWarps) {
+    for (int q = 0; q < nq; ++q) {
       const int s = q % kRawStages, s2 = q % kSplStages;
       bool w = true;
       if (lane == 0) {
@@ -347,8 +353,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
       const double* ra = reinterpret_cast<const double*>(raw + s * kRawStage);
       const double* rb = reinterpret_cast<const double*>(raw + s * kRawStage + kRawA);
       unsigned char* dst = spl + s2 * kSplStage;
-      slice_rows<OZ_M, A_MN>(ra, eA, dst, kPlA, lane);
-      slice_rows<OZ_N, B_MN>(rb, eB, dst + kDigits * kPlA, kPlB, lane);
+      for (int blk = cw; blk < (OZ_M + OZ_N) / 8; blk += kConvWarps) {
+        if (blk < OZ_M / 8) slice_block<OZ_M, A_MN>(ra, eA, dst, kPlA, blk, lane);
+        else slice_block<OZ_N, B_MN>(rb, eB, dst + kDigits * kPlA, kPlB, blk - OZ_M / 8, lane);
+      }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) {
