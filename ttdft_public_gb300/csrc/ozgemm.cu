@@ -29,8 +29,8 @@
 //  - warp 0, one thread: TMA tile loads of the FP64 operands (box 16 x 128 of
 //    A, 16 x 32 of B, either layout) into a raw ring of 3 stages;
 //  - warp 3, one thread: waits for the raw copies in order and publishes the
-//    count of landed chunks (one thread polls the barriers, not five warps);
-//  - warps 4-8, each a fifth of the rows of every chunk: cut the 160 rows x
+//    count of landed chunks (one thread polls the barriers, not eight warps);
+//  - warps 4-11, each an eighth of the rows of every chunk: cut the 160 rows x
 //    16 values into six digit planes each, in the canonical K-major MMA
 //    layout, into a ring of 5 stages;
 //  - warp 2, one thread: waits for the digit planes (and, before a group, for
@@ -38,7 +38,7 @@
 //    publishes the count of ready chunks;
 //  - warp 1, one thread: 21 MMAs (M128 N32 K16) per chunk into the six level
 //    accumulators of one of two buffers;
-//  - warps 9-12 (one per 32 TMEM lanes): fold the levels of each group into
+//  - warps 12-15 (one per 32 TMEM lanes): fold the levels of each group into
 //    running double-FP32 sums in registers; at the end scale by
 //    2^(e_m + e_n - 16) and store.
 // Every wait is bounded; a wait that runs out sets the error word and the
@@ -74,9 +74,9 @@ constexpr int kSplStage = kDigits * (kPlA + kPlB);      // 30 KB
 constexpr int kRawStages = 3;
 constexpr int kSplStages = 5;
 constexpr int kSmem = kRawStages * kRawStage + kSplStages * kSplStage + 1024;
-constexpr int kConvWarp0 = 4, kConvWarps = 5;           // share every chunk's rows
-constexpr int kEpiWarp0 = 9, kEpiWarps = 4;
-constexpr int kThreads = (kEpiWarp0 + kEpiWarps) * 32;  // 416
+constexpr int kConvWarp0 = 4, kConvWarps = 8;           // share every chunk's rows
+constexpr int kEpiWarp0 = 12, kEpiWarps = 4;
+constexpr int kThreads = (kEpiWarp0 + kEpiWarps) * 32;  // 512
 constexpr int kBufCols = kLevels * OZ_N;                // 192
 constexpr uint32_t kTmemCols = 512;                     // two buffers (384)
 
@@ -327,8 +327,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
     }
   } else if (warp >= kConvWarp0 && warp < kConvWarp0 + kConvWarps) {
     // ---- digit planes: every converter warp takes its share of the rows of
-    // every chunk (row blocks of 8: cw, cw + 5, ...), so a chunk's raw stage
-    // is released after a fifth of the work; each warp waits on every phase
+    // every chunk (row blocks of 8: cw, cw + 8, ...), so a chunk's raw stage
+    // is released after an eighth of the work; each warp waits on every phase
     // of the barriers it uses, in order
     const int cw = warp - kConvWarp0;
     for (int q = 0; q < nq; ++q) {

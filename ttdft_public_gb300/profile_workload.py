@@ -3,7 +3,7 @@
     python -m ttdft_public_gb300.profile_workload --workload atoms64 \
         --prec fp32,bf16 --degrees 1 [--rr] [--states K]
     python -m ttdft_public_gb300.profile_workload --workload atoms64 --scf 1 \
-        [--filter mixed]
+        [--filter mixed] [--mix-alpha 0.1] [--history 10]
     python -m ttdft_public_gb300.profile_workload --hartree 3
 
 Builds the workload's operator, uploads a random block and runs `degrees`
@@ -33,6 +33,9 @@ def main():
     ap.add_argument("--rr", action="store_true")
     ap.add_argument("--scf", type=int, default=0)
     ap.add_argument("--filter", default="mixed", choices=("fp64", "fp32", "mixed"))
+    ap.add_argument("--mix-alpha", type=float, default=0.1,
+                    help="Anderson mixing parameter of --scf (the bench's 64-atom setting)")
+    ap.add_argument("--history", type=int, default=10, help="Anderson history of --scf")
     ap.add_argument("--states", type=int, default=0, help="block width (default: the workload's)")
     ap.add_argument("--hartree", type=int, default=0,
                     help="instead: N evaluations of the 35-term Hartree contraction on the "
@@ -48,7 +51,8 @@ def main():
                             cache_dir=os.environ.get("TTG_CACHE"))
     if args.scf:
         from ttdft_public_gb300 import scf
-        res = scf.Scf(s, scf.ScfConfig(max_iter=args.scf, filter=args.filter)).run()
+        res = scf.Scf(s, scf.ScfConfig(max_iter=args.scf, filter=args.filter,
+                                       mix_alpha=args.mix_alpha, history=args.history)).run()
         for h in res["history"]:
             print("iter", h["iter"], "energy", h["energy"], "s", round(h["s"], 3),
                   {k: round(v, 3) for k, v in h["phases"].items()})
