@@ -53,12 +53,16 @@ ttg_status gram_fp64(ttg_op* op, const double* X, const double* Y, int k, double
 }
 
 // out = X Q (transQ = 0) or X Q^T (transQ = 1; lower: Q lower triangular),
-// Q column-major k x k; the same choice of kernel as gram_fp64.
+// Q column-major k x k; the same choice of kernel as gram_fp64.  kscale: Q
+// undoes the columns' scales of X (Q = L^-1 of X's Cholesky-QR); the
+// product then runs on K scales taken from X's columns.
 ttg_status product_fp64(ttg_op* op, const double* X, const double* Q, double* out, int k,
-                        int transQ, bool lower) {
+                        int transQ, bool lower, bool kscale = false) {
   // B(n = q, k = p) = Qop[p, q]: Q[p + q k] (K-major) or, transposed, Q[q + p k] (MN-major)
   const OzOperand A{X, op->n, k, op->ld, false}, B{Q, k, k, k, transQ != 0};
-  if (ozgemm_supported(A, B)) return ozgemm(op, A, B, out, op->ld, 1, false, transQ && lower);
+  const OzOperand cols{X, k, op->n, op->ld, true};
+  if (ozgemm_supported(A, B))
+    return ozgemm(op, A, B, out, op->ld, 1, false, transQ && lower, kscale ? &cols : nullptr);
   return gemm_nn_small(op, X, Q, out, k, transQ, lower);
 }
 
@@ -542,10 +546,9 @@ ttg_status chol_qr_step(ttg_op* op, ttg_block* X, bool shifted) {
   }
   if (shifted) TTG_TRY(scale_cols(op, L, d, k));
   TTG_TRY(kt_begin(op, TTG_KT_ORTH_UPDATE));
-  // X L^-T stays on the double-FP32 kernel: L^-T undoes the columns' scales,
-  // which per-row digit scales of X cannot resolve (a column 1e-6 of the
-  // largest would keep only ~28 of its bits)
-  TTG_TRY(gemm_nn_small(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1, true));
+  // L^-T undoes the columns' scales of X: K scales from those columns keep
+  // a column 1e-6 of the largest at full precision in the digit slicing
+  TTG_TRY(product_fp64(op, X->x.as<double>(), L, op->w64.as<double>(), k, 1, true, true));
   TTG_TRY(kt_end(op));
   std::swap(op->w64.p, X->x.p);
   return TTG_OK;

@@ -91,17 +91,18 @@ __device__ __forceinline__ uint32_t idesc_oz() {
 // 2^-40 resolution of any row whose scale is a normal number); NaN in, NaN out.
 // One 64-bit shift places the 48-bit fixed-point value; the digits come from
 // its two 24-bit halves with 32-bit integer operations.
-__device__ __forceinline__ void digits6(double v, int e, float* d) {
+__device__ __forceinline__ void digits6(double v, int e, int adj, float* d) {
   const int hi = __double2hiint(v);
   const uint32_t lo = (uint32_t)__double2loint(v);
-  const int E = (hi >> 20) & 0x7FF;
+  int E = (hi >> 20) & 0x7FF;
   if (E == 0x7FF) {
 #pragma unroll
     for (int i = 0; i < kDigits; ++i) d[i] = __int_as_float(0x7fc00000);
     return;
   }
   uint32_t xl = 0, xh = 0;
-  if (E != 0) {
+  if (E != 0) E = min(E + adj, 2046);                    // v 2^adj (a K scale)
+  if (E > 0) {
     const unsigned long long M =
         ((unsigned long long)((hi & 0xFFFFF) | 0x100000) << 32) | lo;
     // v 2^(8-e) 2^40 = M 2^(E - 1075 + 48 - e); |v| < 2^e makes the shift >= 5
@@ -167,7 +168,7 @@ __device__ __forceinline__ int plane_off(int row, int k) {
 template <int R, int MN>
 __device__ __forceinline__ void slice_block(const double* __restrict__ raw, const int* es,
                                             unsigned char* planes, int plane_bytes, int rb,
-                                            int lane) {
+                                            int lane, const int* __restrict__ kadj, int ksign) {
   const int row = 8 * rb + (lane >> 2), kp = lane & 3;
   const int e = es[row];
   double v[2][2];
@@ -187,8 +188,10 @@ __device__ __forceinline__ void slice_block(const double* __restrict__ raw, cons
   for (int kh = 0; kh < 2; ++kh) {
     const int k = 8 * kh + 2 * kp;
     float d0[kDigits], d1[kDigits];
-    digits6(v[kh][0], e, d0);
-    digits6(v[kh][1], e, d1);
+    const int a0 = kadj ? ksign * __ldg(kadj + k) : 0;
+    const int a1 = kadj ? ksign * __ldg(kadj + k + 1) : 0;
+    digits6(v[kh][0], e, a0, d0);
+    digits6(v[kh][1], e, a1, d1);
     const int off = plane_off(row, k);
 #pragma unroll
     for (int d = 0; d < kDigits; ++d)
@@ -221,7 +224,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
     const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
     const int* __restrict__ expA, const int* __restrict__ expB, int M, int N, int K,
     int k_per_split, int b_lower, OzTiles tiles, double* __restrict__ out, int64_t o_rs,
-    int64_t o_cs, int64_t o_zs, int* __restrict__ err) {
+    int64_t o_cs, int64_t o_zs, const int* __restrict__ kexp, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((1024 - (su32(smem_raw) & 1023)) & 1023);
   unsigned char* raw = smem;                                  // kRawStages x 20 KB
@@ -354,8 +357,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
       const double* rb = reinterpret_cast<const double*>(raw + s * kRawStage + kRawA);
       unsigned char* dst = spl + s2 * kSplStage;
       for (int blk = cw; blk < (OZ_M + OZ_N) / 8; blk += kConvWarps) {
-        if (blk < OZ_M / 8) slice_block<OZ_M, A_MN>(ra, eA, dst, kPlA, blk, lane);
-        else slice_block<OZ_N, B_MN>(rb, eB, dst + kDigits * kPlA, kPlB, blk - OZ_M / 8, lane);
+        // K scales of this chunk (K values beyond the operands are zero)
+        const int* kq = kexp ? kexp + (k0 + q * OZ_K) : nullptr;
+        if (blk < OZ_M / 8) slice_block<OZ_M, A_MN>(ra, eA, dst, kPlA, blk, lane, kq, -1);
+        else slice_block<OZ_N, B_MN>(rb, eB, dst + kDigits * kPlA, kPlB, blk - OZ_M / 8, lane, kq,
+                                     1);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
@@ -494,31 +500,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozgemm(
 // Row scales: e[r] with max_k |A(r, k)| < 2^e[r] (0 for an all-zero row), from
 // the largest biased exponent of the row: any v with biased exponent E is
 // below 2^(E - 1022).  ebits[r] (zeroed by the caller) collects the maxima.
+// With K scales (kexp, ksign): the biased exponent of v 2^(ksign kexp[k]).
+__device__ __forceinline__ int scaled_ebits(double v, const int* kexp, int ksign, int64_t k) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  int E = (int)((b >> 52) & 0x7FF);
+  if (E != 0 && E != 0x7FF && kexp) E = max(0, min(2046, E + ksign * __ldg(kexp + k)));
+  return E;
+}
+
 __global__ void k_rowexp_mn(const double* __restrict__ p, int64_t rows, int64_t kext, int64_t ld,
-                            int64_t k_per_block, int* __restrict__ ebits) {
+                            int64_t k_per_block, const int* __restrict__ kexp, int ksign,
+                            int* __restrict__ ebits) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= rows) return;
   const int64_t k0 = (int64_t)blockIdx.y * k_per_block;
   const int64_t k1 = min(kext, k0 + k_per_block);
   int m = 0;
-  for (int64_t k = k0; k < k1; ++k) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(p[k * ld + r]);
-    m = max(m, (int)((b >> 52) & 0x7FF));
-  }
+  for (int64_t k = k0; k < k1; ++k) m = max(m, scaled_ebits(p[k * ld + r], kexp, ksign, k));
   if (m) atomicMax(ebits + r, m);
 }
 
 // K-major rows: one warp per row
 __global__ void k_rowexp_k(const double* __restrict__ p, int64_t rows, int64_t kext, int64_t ld,
-                           int* __restrict__ ebits) {
+                           const int* __restrict__ kexp, int ksign, int* __restrict__ ebits) {
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= rows) return;
   int m = 0;
-  for (int64_t k = lane; k < kext; k += 32) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(p[r * ld + k]);
-    m = max(m, (int)((b >> 52) & 0x7FF));
-  }
+  for (int64_t k = lane; k < kext; k += 32) m = max(m, scaled_ebits(p[r * ld + k], kexp, ksign, k));
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0) ebits[r] = m;
 }
@@ -593,15 +602,16 @@ ttg_status make_map(CUtensorMap* map, const OzOperand& o, int box_rows) {
   return r == CUDA_SUCCESS ? TTG_OK : TTG_BAD_ARG;
 }
 
-ttg_status row_exps(cudaStream_t st, const OzOperand& o, int* e) {
+ttg_status row_exps(cudaStream_t st, const OzOperand& o, int* e, const int* kexp = nullptr,
+                    int ksign = 0) {
   TTG_CUDA_TRY(cudaMemsetAsync(e, 0, (size_t)o.rows * sizeof(int), st));
   if (o.mn_major) {
     const int64_t kb = 4096;
     dim3 grid((unsigned)((o.rows + 255) / 256), (unsigned)((o.kext + kb - 1) / kb));
-    k_rowexp_mn<<<grid, 256, 0, st>>>(o.p, o.rows, o.kext, o.ld, kb, e); TTG_COUNT();
+    k_rowexp_mn<<<grid, 256, 0, st>>>(o.p, o.rows, o.kext, o.ld, kb, kexp, ksign, e); TTG_COUNT();
   } else {
     k_rowexp_k<<<(unsigned)((o.rows * 32 + 255) / 256), 256, 0, st>>>(o.p, o.rows, o.kext, o.ld,
-                                                                     e); TTG_COUNT();
+                                                                     kexp, ksign, e); TTG_COUNT();
   }
   TTG_CUDA_TRY(cudaGetLastError());
   k_exp_from_bits<<<(unsigned)((o.rows + 255) / 256), 256, 0, st>>>(e, o.rows); TTG_COUNT();
@@ -612,7 +622,8 @@ ttg_status row_exps(cudaStream_t st, const OzOperand& o, int* e) {
 template <int A_MN, int B_MN>
 ttg_status launch(dim3 grid, cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb,
                   const int* ea, const int* eb, int M, int N, int K, int kps, int b_lower,
-                  OzTiles tiles, double* out, int64_t o_rs, int64_t o_cs, int64_t o_zs, int* err) {
+                  OzTiles tiles, double* out, int64_t o_rs, int64_t o_cs, int64_t o_zs,
+                  const int* kexp, int* err) {
   static std::once_flag once;
   static cudaError_t attr = cudaSuccess;
   std::call_once(once, [] {
@@ -621,7 +632,7 @@ ttg_status launch(dim3 grid, cudaStream_t st, const CUtensorMap& ma, const CUten
   });
   if (attr != cudaSuccess) return TTG_CUDA_ERR;
   k_ozgemm<A_MN, B_MN><<<grid, kThreads, kSmem, st>>>(ma, mb, ea, eb, M, N, K, kps, b_lower,
-                                                     tiles, out, o_rs, o_cs, o_zs, err);
+                                                     tiles, out, o_rs, o_cs, o_zs, kexp, err);
   TTG_COUNT();
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && sync_launches()) e = cudaStreamSynchronize(st);
@@ -642,7 +653,7 @@ bool ozgemm_supported(const OzOperand& A, const OzOperand& B) {
 }
 
 ttg_status ozgemm(ttg_op* op, const OzOperand& A, const OzOperand& B, double* C, int64_t c_rs,
-                  int64_t c_cs, bool sym, bool b_lower) {
+                  int64_t c_cs, bool sym, bool b_lower, const OzOperand* kscale_of) {
   if (!ozgemm_supported(A, B) || !C) return TTG_BAD_ARG;
   if (sym && A.rows != B.rows) return TTG_BAD_ARG;
   cudaStream_t st = op->stream;
@@ -655,8 +666,20 @@ ttg_status ozgemm(ttg_op* op, const OzOperand& A, const OzOperand& B, double* C,
   }
   int* ea = op->oz_exp.as<int>();
   int* eb = ea + M;
-  TTG_TRY(row_exps(st, A, ea));
-  TTG_TRY(row_exps(st, B, eb));
+  // K scales: the row scales of kscale_of (an MN-major view whose rows are
+  // the K index), A scaled by 2^-f_k and B by 2^f_k; the buffer is padded
+  // with zeros to whole chunks
+  const int* kexp = nullptr;
+  if (kscale_of) {
+    if (kscale_of->rows != K) return TTG_BAD_ARG;
+    const size_t kb = (size_t)((K + OZ_K - 1) / OZ_K * OZ_K) * sizeof(int);
+    if (op->oz_kexp.bytes < kb) TTG_TRY(op->oz_kexp.alloc(kb));
+    TTG_CUDA_TRY(cudaMemsetAsync(op->oz_kexp.p, 0, kb, st));
+    TTG_TRY(row_exps(st, *kscale_of, op->oz_kexp.as<int>()));
+    kexp = op->oz_kexp.as<int>();
+  }
+  TTG_TRY(row_exps(st, A, ea, kexp, -1));
+  TTG_TRY(row_exps(st, B, eb, kexp, 1));
   CUtensorMap ma, mb;
   TTG_TRY(make_map(&ma, A, OZ_M));
   TTG_TRY(make_map(&mb, B, OZ_N));
@@ -688,13 +711,13 @@ ttg_status ozgemm(ttg_op* op, const OzOperand& A, const OzOperand& B, double* C,
   int* err = op->oz_err.as<int>();
   const int bl = b_lower ? 1 : 0;
   if (A.mn_major && B.mn_major)
-    TTG_TRY((launch<1, 1>(grid, st, ma, mb, ea, eb, M, N, K, kps, bl, tiles, out, o_rs, o_cs, zs, err)));
+    TTG_TRY((launch<1, 1>(grid, st, ma, mb, ea, eb, M, N, K, kps, bl, tiles, out, o_rs, o_cs, zs, kexp, err)));
   else if (A.mn_major)
-    TTG_TRY((launch<1, 0>(grid, st, ma, mb, ea, eb, M, N, K, kps, bl, tiles, out, o_rs, o_cs, zs, err)));
+    TTG_TRY((launch<1, 0>(grid, st, ma, mb, ea, eb, M, N, K, kps, bl, tiles, out, o_rs, o_cs, zs, kexp, err)));
   else if (B.mn_major)
-    TTG_TRY((launch<0, 1>(grid, st, ma, mb, ea, eb, M, N, K, kps, bl, tiles, out, o_rs, o_cs, zs, err)));
+    TTG_TRY((launch<0, 1>(grid, st, ma, mb, ea, eb, M, N, K, kps, bl, tiles, out, o_rs, o_cs, zs, kexp, err)));
   else
-    TTG_TRY((launch<0, 0>(grid, st, ma, mb, ea, eb, M, N, K, kps, bl, tiles, out, o_rs, o_cs, zs, err)));
+    TTG_TRY((launch<0, 0>(grid, st, ma, mb, ea, eb, M, N, K, kps, bl, tiles, out, o_rs, o_cs, zs, kexp, err)));
   if (out != C) {
     const int64_t mn = (int64_t)M * N;
     k_oz_reduce<<<(unsigned)std::min<int64_t>((mn + 255) / 256, 4096), 256, 0, st>>>(

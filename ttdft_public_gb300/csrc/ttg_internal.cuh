@@ -226,6 +226,7 @@ struct ttg_op {
   ttg::DevBuf kk3;            // eigensolver scratch (k*k + 6k doubles)
   ttg::DevBuf chol;           // blocked Cholesky: the diagonal before factorisation
   ttg::DevBuf oz_exp;         // FP64 tensor-core GEMM: row scales of its operands
+  ttg::DevBuf oz_kexp;        // FP64 tensor-core GEMM: K scales (padded to whole chunks)
   ttg::DevBuf oz_err;         // FP64 tensor-core GEMM: error word
   ttg::DevBuf eigbuf;         // eigensolver refinement (5 k*k doubles)
   ttg::DevBuf eigf;           // FP32 tridiagonalisation scratch
@@ -353,8 +354,13 @@ bool ozgemm_supported(const OzOperand& A, const OzOperand& B);
 // C[m c_rs + n c_cs] = sum_k A(m, k) B(n, k).  sym: A B^T is symmetric (A = B,
 // or B = H A): only tiles on and below the diagonal are computed and the
 // others mirrored.  b_lower: B(n, k) = 0 for k > n (the sum stops at n).
+// kscale_of: an MN-major operand whose rows are the K index (K of them);
+// with power-of-two scales f_k = its row scales, A is sliced as
+// A(m, k) 2^-f_k and B as B(n, k) 2^f_k, which leaves A B^T unchanged and
+// keeps small K columns of A (that B amplifies) at full precision.
 ttg_status ozgemm(ttg_op* op, const OzOperand& A, const OzOperand& B, double* C, int64_t c_rs,
-                  int64_t c_cs, bool sym, bool b_lower = false);
+                  int64_t c_cs, bool sym, bool b_lower = false,
+                  const OzOperand* kscale_of = nullptr);
 // Reads and clears the tensor-core GEMM's error word (synchronises).
 ttg_status ozgemm_error(ttg_op* op);
 
