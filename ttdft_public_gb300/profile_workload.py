@@ -5,6 +5,7 @@
     python -m ttdft_public_gb300.profile_workload --workload atoms64 --scf 1 \
         [--filter mixed] [--mix-alpha 0.1] [--history 10]
     python -m ttdft_public_gb300.profile_workload --hartree 3
+    python -m ttdft_public_gb300.profile_workload --gram 64000,256,3
 
 Builds the workload's operator, uploads a random block and runs `degrees`
 filter degrees per listed precision (one fused SpMM launch each) and, with
@@ -37,10 +38,30 @@ def main():
                     help="Anderson mixing parameter of --scf (the bench's 64-atom setting)")
     ap.add_argument("--history", type=int, default=10, help="Anderson history of --scf")
     ap.add_argument("--states", type=int, default=0, help="block width (default: the workload's)")
+    ap.add_argument("--gram", default="",
+                    help="instead: N,K,reps: X^T Y of two random N x K blocks (ttg_gram, the FP64 "
+                         "tensor-core GEMM) on an identity operator, reps times")
     ap.add_argument("--hartree", type=int, default=0,
                     help="instead: N evaluations of the 35-term Hartree contraction on the "
                          "standalone workload (core 60^3, 360 points per direction)")
     args = ap.parse_args()
+    if args.gram:
+        import ctypes
+        import time
+        from ttdft_public_gb300 import _lib
+        n, k, reps = (int(x) for x in args.gram.split(","))
+        H = system.Csr(n, n, np.arange(n + 1, dtype=np.int64), np.arange(n, dtype=np.int32),
+                       np.ones(n))
+        op = api.Operator(api.ProjectHamiltonianSparse(H), k)
+        rng = np.random.default_rng(0)
+        X = api.Mat(op, k, rng.standard_normal((n, k)))
+        Y = api.Mat(op, k, rng.standard_normal((n, k)))
+        S = np.zeros((k, k), order="F")
+        for _ in range(reps):
+            t = time.perf_counter()
+            assert _lib.ttg().ttg_gram(op.h, X.h, Y.h, ctypes.c_void_p(S.ctypes.data)) == 0
+            print(f"gram {n} x {k}: {(time.perf_counter() - t) * 1e3:.2f} ms")
+        return
     if args.hartree:
         case = system.hartree_blob_case()
         for _ in range(args.hartree):
