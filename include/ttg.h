@@ -186,11 +186,16 @@ ttg_status ttg_apply_h(ttg_op* op, const ttg_block* X, ttg_block* HX);
 
 /* S = X^T Y (k x k, column-major).  Replaces MultTM::mult
  * (eigensolver/MultTm.h:37, eigensolver/MultTm.cu:86-224).  FP64 data and
- * result; the products and sums run in double-FP32 arithmetic (each value a
- * pair of floats, about 47 significant bits, FP32 exponent range): an entry
- * lands within ~6e-14 of the sum of |terms| of its dot product, where native
- * FP64 would reach ~1e-16 x length.  s_host may be NULL when only the device
- * copy is wanted (kept inside the op). */
+ * result, computed on the tensor cores: each value becomes six exact BF16
+ * digits on a power-of-two scale of its row, the digit products are summed
+ * exactly in tensor memory and the 96-deep groups in double-FP32, so an entry
+ * lands within about 2^-48 of the product of its two rows' scales times the
+ * length (measured: within 2^-44 of the sum of |terms|).  When an operand's
+ * alignment rules the tensor cores out, the products and sums run in
+ * double-FP32 on the CUDA cores (each value a pair of floats, about 47
+ * significant bits, FP32 exponent range; within ~6e-14 of the sum of |terms|).
+ * s_host may be NULL when only the device copy is wanted (kept inside the
+ * op). */
 ttg_status ttg_gram(ttg_op* op, const ttg_block* X, const ttg_block* Y, double* s_host);
 
 /* S = X^T Y like ttg_gram, for callers that cannot allocate device memory
@@ -200,8 +205,8 @@ ttg_status ttg_gram(ttg_op* op, const ttg_block* X, const ttg_block* Y, double* 
  * dimension ld; S is a device pointer, k x k column-major; stream may be NULL.
  * Allocates nothing: the split-row partial sums live in a fixed 16 MiB
  * __device__ array that every GPU loading this library holds until exit, so
- * k*k must not exceed 2,097,152 (k <= 1448), else TTG_BAD_ARG.  Arithmetic as
- * ttg_gram (double-FP32, about 47 bits).  The first call on a device looks up
+ * k*k must not exceed 2,097,152 (k <= 1448), else TTG_BAD_ARG.  Arithmetic:
+ * double-FP32 (about 47 bits), the fallback path of ttg_gram.  The first call on a device looks up
  * the array's address (with lazy module loading this also loads the library's
  * device code and commits the array), so make it at start-up, before any
  * stream capture and before the host's no-allocation phase begins.  The
@@ -213,10 +218,12 @@ ttg_status ttg_gram_noalloc(const double* x_dev, const double* y_dev, int64_t n,
 
 /* Cholesky-QR: S = X^T X = L L^T, X <- X L^-T.  Replaces MultTM::orth
  * (eigensolver/MultTm.h:39, eigensolver/MultTm.cu:226-467).  The Gram matrix
- * S and the product X L^-T are double-FP32 (about 47 bits, see ttg_gram); the
- * Cholesky factorisation and L^-1 are FP64.  Orthogonality therefore degrades
- * at condition numbers of X roughly 8x smaller than with native FP64 (the
- * orthogonality error grows as cond(X)^2 times the Gram's relative error).
+ * S and the product X L^-T run as ttg_gram does (tensor cores, about 2^-48
+ * relative to the row scales; X L^-T also scales X's columns to powers of two
+ * first, since L^-T undoes them); the Cholesky factorisation and L^-1 are
+ * FP64 (blocked on many CTAs for k > 128).  Orthogonality degrades with
+ * cond(X)^2 times the Gram's relative error, a few times sooner than with
+ * native FP64.
  * Returns TTG_NOT_SPD (X untouched) when S is not numerically positive
  * definite. */
 ttg_status ttg_chol_qr(ttg_op* op, ttg_block* X);
