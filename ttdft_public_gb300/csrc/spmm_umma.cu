@@ -135,7 +135,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity,
         : "r"(smem_u32(b)), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (stop && *stop) return false;
+    // the abort flag is read once per 32 polls: a shared-memory load in every
+    // poll slows the mbarrier operations of the whole CTA
+    if (stop && (i & 31) == 31 && *stop) return false;
   }
   return false;
 }
@@ -153,7 +155,7 @@ __device__ __forceinline__ bool mbar_wait_idle(uint64_t* b, uint32_t parity, int
         : "r"(smem_u32(b)), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (stop && *stop) return false;
+    if (stop && (i & 7) == 7 && *stop) return false;
     __nanosleep(ns);
   }
   return false;
@@ -406,7 +408,7 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
       for (int i = 0; i < kMaxWait && avail <= (uint32_t)c; ++i) {
         asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(avail) : "r"(smem_u32(&ready))
                      : "memory");
-        if (avail <= (uint32_t)c && abort_flag) break;
+        if (avail <= (uint32_t)c && (i & 31) == 31 && abort_flag) break;
       }
       if (avail <= (uint32_t)c) {
         ok = false;
