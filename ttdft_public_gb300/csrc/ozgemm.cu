@@ -606,7 +606,7 @@ ttg_status row_exps(cudaStream_t st, const OzOperand& o, int* e, const int* kexp
                     int ksign = 0) {
   TTG_CUDA_TRY(cudaMemsetAsync(e, 0, (size_t)o.rows * sizeof(int), st));
   if (o.mn_major) {
-    const int64_t kb = 4096;
+    const int64_t kb = 256;                 // enough CTAs for a narrow block of many rows
     dim3 grid((unsigned)((o.rows + 255) / 256), (unsigned)((o.kext + kb - 1) / kb));
     k_rowexp_mn<<<grid, 256, 0, st>>>(o.p, o.rows, o.kext, o.ld, kb, kexp, ksign, e); TTG_COUNT();
   } else {
@@ -679,7 +679,11 @@ ttg_status ozgemm(ttg_op* op, const OzOperand& A, const OzOperand& B, double* C,
     kexp = op->oz_kexp.as<int>();
   }
   TTG_TRY(row_exps(st, A, ea, kexp, -1));
-  TTG_TRY(row_exps(st, B, eb, kexp, 1));
+  if (!kexp && B.p == A.p && B.rows == A.rows && B.kext == A.kext && B.ld == A.ld &&
+      B.mn_major == A.mn_major)
+    TTG_CUDA_TRY(cudaMemcpyAsync(eb, ea, (size_t)M * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  else
+    TTG_TRY(row_exps(st, B, eb, kexp, 1));
   CUtensorMap ma, mb;
   TTG_TRY(make_map(&ma, A, OZ_M));
   TTG_TRY(make_map(&mb, B, OZ_N));
