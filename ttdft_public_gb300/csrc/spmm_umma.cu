@@ -41,12 +41,7 @@
 // BF16 block's rows as they are, issue one MMA per chunk and round the
 // epilogue's FP32 result to BF16.
 // Every wait (mbarrier or the ready count) is bounded; a wait that runs out
-// sets an error word and the CTA's abort flag.  On abort no role issues new
-// copies or MMAs: the H thread stops and publishes how many H copies it
-// issued, the row warps arrive (without copying) on the chunks they still
-// owe below that count, the wait thread waits for those chunks' barriers so
-// that every issued copy has landed, and the MMA thread commits what it has
-// issued; then the CTA frees its tensor memory and exits as usual.
+// sets an error word.
 
 #include <cuda_bf16.h>
 
@@ -123,9 +118,7 @@ __device__ __forceinline__ void mbar_init(uint64_t* b, int count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
 }
 
-// stop (may be null): a flag that ends the wait early, unsuccessfully
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity,
-                                          const volatile int* stop = nullptr) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
   for (int i = 0; i < kMaxWait; ++i) {
     uint32_t ok;
     asm volatile(
@@ -135,17 +128,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity,
         : "r"(smem_u32(b)), "r"(parity)
         : "memory");
     if (ok) return true;
-    // the abort flag is read once per 32 polls: a shared-memory load in every
-    // poll slows the mbarrier operations of the whole CTA
-    if (stop && (i & 31) == 31 && *stop) return false;
   }
   return false;
 }
 
 // For waits off the critical path: a thread that polls an mbarrier without
 // pause slows the mbarrier operations of the threads that are on it.
-__device__ __forceinline__ bool mbar_wait_idle(uint64_t* b, uint32_t parity, int ns,
-                                               const volatile int* stop = nullptr) {
+__device__ __forceinline__ bool mbar_wait_idle(uint64_t* b, uint32_t parity, int ns) {
   for (int i = 0; i < kMaxWait; ++i) {
     uint32_t ok;
     asm volatile(
@@ -155,21 +144,9 @@ __device__ __forceinline__ bool mbar_wait_idle(uint64_t* b, uint32_t parity, int
         : "r"(smem_u32(b)), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (stop && (i & 7) == 7 && *stop) return false;
     __nanosleep(ns);
   }
   return false;
-}
-
-// The count of chunks whose H copy was issued, once the H thread has stopped
-// (-1 before); -1 if it does not come within the bound.
-__device__ __forceinline__ int wait_h_final(const volatile int* h_final) {
-  int hf = *h_final;
-  for (int i = 0; i < kMaxWait && hf < 0; ++i) {
-    __nanosleep(64);
-    hf = *h_final;
-  }
-  return hf;
 }
 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
@@ -201,8 +178,6 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
   __shared__ __align__(8) uint64_t accf;     // all MMAs of the tile done (one phase)
   __shared__ uint32_t tmem_slot;
   __shared__ uint32_t ready;                 // chunks whose two stages are full
-  __shared__ volatile int abort_flag;        // a wait ran out: issue nothing new
-  __shared__ volatile int h_final;           // H copies issued, once the H thread stops
   // tiles in decreasing chunk count, so the longest start first and the short
   // ones fill the tail of the launch
   const int tile = __ldg(order + blockIdx.x), tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -227,8 +202,6 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     }
     mbar_init(&accf, 1);
     ready = 0;
-    abort_flag = 0;
-    h_final = -1;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -244,19 +217,13 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     if (lane == 0) {
       uint64_t pol_stream;
       asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol_stream));
-      int c = 0;
-      for (; c < nch; ++c) {
-        if (abort_flag) break;
+      for (int c = 0; c < nch; ++c) {
         const int s = c % nh;
         // one wait per two chunks: the MMAs complete in order, so chunk
         // c + 1 - nh done means chunk c - nh is done too
         if (c >= nh && ((c - nh) & 1) == 0) {
           const int x = (c + 1 < nch ? c + 1 : c) - nh;
-          if (!mbar_wait(&done[x % nd], (x / nd) & 1, &abort_flag)) {
-            ok = false;
-            abort_flag = 1;
-            break;
-          }
+          ok &= mbar_wait(&done[x % nd], (x / nd) & 1);
         }
         const uint32_t fb = smem_u32(&full[c % nd]);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb),
@@ -268,10 +235,6 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
               "r"(HB), "r"(fb), "l"(pol_stream)
             : "memory");
       }
-      // issuing chunk c needed chunk c - nh's MMAs done, hence every chunk
-      // up to c - nh ready: for each c < h_final the previous phase of
-      // full[c % nd] has completed, so the row warps may arrive on it
-      h_final = c;
     }
   } else if (warp >= kFirstBWarp) {
     // gathered rows: warps kFirstBWarp.. (pw = 0 .. np-1) take whole chunks in
@@ -299,7 +262,6 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
         const int c = pw + j * np;
         cur[j] = c < nch ? __ldg(colp + (int64_t)c * UK) : 0;
       }
-      int owed = nch;          // this warp's first chunk not arrived on, after an abort
       for (int c0 = pw; c0 < nch; c0 += kColAhead * np) {
 #pragma unroll
         for (int j = 0; j < kColAhead; ++j) {
@@ -311,17 +273,7 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
           const int c = c0 + j * np;
           if (c >= nch) break;
           const int s = c % nb;
-          bool go = !abort_flag;
-          if (go && c >= nb && !mbar_wait_idle(&done[(c - nb) % nd], ((c - nb) / nd) & 1, 64,
-                                               &abort_flag)) {
-            ok = false;
-            abort_flag = 1;
-            go = false;
-          }
-          if (__any_sync(0xffffffffu, !go)) {
-            owed = c;
-            goto rows_stop;
-          }
+          if (c >= nb) ok &= mbar_wait_idle(&done[(c - nb) % nd], ((c - nb) / nd) & 1, 64);
           const uint32_t sb = smem_u32(smem + s * bstage);
 #pragma unroll
           for (int rq = 0; rq < 4; ++rq) {
@@ -352,41 +304,17 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
 #pragma unroll
         for (int j = 0; j < kColAhead; ++j) cur[j] = nxt[j];
       }
-    rows_stop:
       cp_async_wait<0>();
-      if (owed < nch && lane == 0) {
-        // abort: arrive, without copying, on the chunks this warp still owes
-        // among those whose H copy was issued, so that their barriers complete
-        // once the copies land
-        const int hf = wait_h_final(&h_final);
-        if (hf < 0) ok = false;
-        for (int c = owed; c < hf; c += np)
-          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full[c % nd]))
-                       : "memory");
-      }
     }
   } else if (warp == kWaitWarp) {
     // waits for each chunk's stages to fill, in order, and publishes the count of
     // ready chunks to the MMA thread: an mbarrier wait by the MMA-issuing
     // thread itself queues behind its outstanding MMAs (about 0.1 us a chunk)
     if (lane == 0) {
-      int c = 0;
-      for (; c < nch; ++c) {
-        if (!mbar_wait(&full[c % nd], (c / nd) & 1, &abort_flag)) {
-          ok = false;
-          abort_flag = 1;
-          break;
-        }
+      for (int c = 0; c < nch; ++c) {
+        ok &= mbar_wait(&full[c % nd], (c / nd) & 1);
         asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"(smem_u32(&ready)), "r"(c + 1)
                      : "memory");
-      }
-      if (c < nch) {
-        // abort: wait (bounded) until every H copy that was issued has
-        // landed; chunks below h_final get their row arrivals from the row
-        // warps, and no MMA reads them any more
-        const int hf = wait_h_final(&h_final);
-        if (hf < 0) ok = false;
-        for (; c < hf; ++c) ok &= mbar_wait(&full[c % nd], (c / nd) & 1);
       }
     }
   } else if (warp == kMmaWarp && lane == 0) {
@@ -405,16 +333,10 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
     int sd = 0;
     uint32_t avail = 0;
     for (int c = 0; c < nch; ++c) {
-      for (int i = 0; i < kMaxWait && avail <= (uint32_t)c; ++i) {
+      for (int i = 0; i < kMaxWait && avail <= (uint32_t)c; ++i)
         asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(avail) : "r"(smem_u32(&ready))
                      : "memory");
-        if (avail <= (uint32_t)c && (i & 31) == 31 && abort_flag) break;
-      }
-      if (avail <= (uint32_t)c) {
-        ok = false;
-        abort_flag = 1;
-        break;
-      }
+      ok &= avail > (uint32_t)c;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       // (term of A, term of B): (1,1) (0,2) (2,0) (0,1) (1,0) (0,0)
       const uint64_t da[6] = {da_hi | (a_lo + apl), da_hi | a_lo, da_hi | (a_lo + 2 * apl),
@@ -440,7 +362,6 @@ __global__ void __launch_bounds__(kThreads) k_cheb_umma(
       if (b_lo == b_end) b_lo = b_first;
       if (++sd == nd) sd = 0;
     }
-    // after an abort too: the commit tracks every MMA issued so far
     if (nch > 0)
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
