@@ -60,8 +60,9 @@ def _has_gpu():
 
 def test_host_library_exports():
     lib = _lib.host()
-    assert hasattr(lib, "ttg_host_assemble_hloc")
-    assert hasattr(lib, "ttg_host_assemble_cnloc")
+    for name in ("ttg_host_assemble_hloc", "ttg_host_assemble_hloc_once",
+                 "ttg_host_assemble_hloc_pattern", "ttg_host_assemble_cnloc", "ttg_host_free"):
+        assert hasattr(lib, name)
 
 
 def test_cxx_classes_build_and_export():

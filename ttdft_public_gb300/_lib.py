@@ -37,7 +37,7 @@ def host():
             build.build_host()
         _host = ctypes.CDLL(path)
         for name in ("ttg_host_assemble_hloc", "ttg_host_assemble_cnloc",
-                     "ttg_host_assemble_hloc_once"):
+                     "ttg_host_assemble_hloc_once", "ttg_host_assemble_hloc_pattern"):
             getattr(_host, name).restype = ctypes.c_int
         _host.ttg_host_free.restype = None
         _host.ttg_host_free.argtypes = [ctypes.c_void_p]

@@ -57,16 +57,23 @@ Sparse1D make_sparse(const double* m, int r, double drop) {
   return s;
 }
 
-// Scratch of one thread: a dense row accumulator and the list of touched columns.
+// Scratch of one thread: a dense row accumulator, a second one for the
+// pattern-only potential (when there is one) and the list of touched columns.
 struct RowScratch {
-  std::vector<double> row;
+  std::vector<double> row, extra;
   std::vector<char> touched;
   std::vector<int> touched_list;
-  explicit RowScratch(int64_t n) : row(n, 0.0), touched(n, 0) { touched_list.reserve(1 << 16); }
+  RowScratch(int64_t n, bool with_extra)
+      : row(n, 0.0), extra(with_extra ? n : 0, 0.0), touched(n, 0) {
+    touched_list.reserve(1 << 16);
+  }
 };
 
 // Builds one row of H_loc: the kinetic and potential Kronecker sums, then
-// the entries above the truncation in column order.
+// the entries above the truncation in column order.  An optional second CP
+// potential (npat terms) widens the pattern only: an entry is kept when its
+// value, or its value with that potential added, exceeds the truncation, and
+// the value stored leaves the second potential out.
 struct RowBuilder {
   int rx, ry, rz;
   int64_t N;
@@ -74,18 +81,25 @@ struct RowBuilder {
   const std::vector<Sparse1D>*sPX, *sPY, *sPZ;
   int nterm;
   const double* coef;
+  const std::vector<Sparse1D>*sQX, *sQY, *sQZ;
+  int npat;
+  const double* pcoef;
   double truncation, prune;
 
   void row(int64_t I, RowScratch& s, std::vector<int>& out_cols,
            std::vector<double>& out_vals) const {
     std::vector<double>& row = s.row;
+    std::vector<double>& extra = s.extra;
     std::vector<char>& touched = s.touched;
     std::vector<int>& touched_list = s.touched_list;
-    auto add = [&](int64_t J, double v) {
+    auto touch = [&](int64_t J) {
       if (!touched[J]) {
         touched[J] = 1;
         touched_list.push_back((int)J);
       }
+    };
+    auto add = [&](int64_t J, double v) {
+      touch(J);
       row[J] += v;
     };
       const int xI = (int)(I % rx);
@@ -110,29 +124,43 @@ struct RowBuilder {
           }
         }
       }
-      // potential: sum_t coef_t PX_t PY_t PZ_t
-      for (int t = 0; t < nterm; ++t) {
-        const Sparse1D &px = (*sPX)[t], &py = (*sPY)[t], &pz = (*sPZ)[t];
-        const double bound = std::fabs(coef[t]) * px.rowmax[xI] * py.rowmax[yI] * pz.rowmax[zI];
-        if (bound <= prune) continue;
-        for (int64_t qz = pz.ptr[zI]; qz < pz.ptr[zI + 1]; ++qz) {
-          const int zJ = pz.col[qz];
-          const double wz = coef[t] * pz.val[qz];
-          if (std::fabs(wz) * py.rowmax[yI] * px.rowmax[xI] <= prune) continue;
-          for (int64_t qy = py.ptr[yI]; qy < py.ptr[yI + 1]; ++qy) {
-            const int yJ = py.col[qy];
-            const double w = wz * py.val[qy];
-            if (std::fabs(w) * px.rowmax[xI] <= prune) continue;
-            const int64_t base = (int64_t)rx * (yJ + (int64_t)ry * zJ);
-            for (int64_t qx = px.ptr[xI]; qx < px.ptr[xI + 1]; ++qx)
-              add(base + px.col[qx], w * px.val[qx]);
+      // potential: sum_t c_t PX_t PY_t PZ_t, into `acc`
+      auto add_cp = [&](const std::vector<Sparse1D>& PX, const std::vector<Sparse1D>& PY,
+                        const std::vector<Sparse1D>& PZ, int n, const double* c,
+                        std::vector<double>& acc) {
+        for (int t = 0; t < n; ++t) {
+          const Sparse1D &px = PX[t], &py = PY[t], &pz = PZ[t];
+          const double bound = std::fabs(c[t]) * px.rowmax[xI] * py.rowmax[yI] * pz.rowmax[zI];
+          if (bound <= prune) continue;
+          for (int64_t qz = pz.ptr[zI]; qz < pz.ptr[zI + 1]; ++qz) {
+            const int zJ = pz.col[qz];
+            const double wz = c[t] * pz.val[qz];
+            if (std::fabs(wz) * py.rowmax[yI] * px.rowmax[xI] <= prune) continue;
+            for (int64_t qy = py.ptr[yI]; qy < py.ptr[yI + 1]; ++qy) {
+              const int yJ = py.col[qy];
+              const double w = wz * py.val[qy];
+              if (std::fabs(w) * px.rowmax[xI] <= prune) continue;
+              const int64_t base = (int64_t)rx * (yJ + (int64_t)ry * zJ);
+              for (int64_t qx = px.ptr[xI]; qx < px.ptr[xI + 1]; ++qx) {
+                const int64_t J = base + px.col[qx];
+                touch(J);
+                acc[J] += w * px.val[qx];
+              }
+            }
           }
         }
-      }
+      };
+      add_cp(*sPX, *sPY, *sPZ, nterm, coef, row);
+      if (npat > 0) add_cp(*sQX, *sQY, *sQZ, npat, pcoef, extra);
       std::sort(touched_list.begin(), touched_list.end());
       for (int J : touched_list) {
         const double v = row[J];
-        if (std::fabs(v) > truncation) {
+        bool keep = std::fabs(v) > truncation;
+        if (npat > 0) {
+          keep = keep || std::fabs(v + extra[J]) > truncation;
+          extra[J] = 0.0;
+        }
+        if (keep) {
           out_cols.push_back(J);
           out_vals.push_back(v);
         }
@@ -142,6 +170,12 @@ struct RowBuilder {
       touched_list.clear();
   }
 };
+
+std::vector<Sparse1D> sparse_terms(const double* P, int n, int r, double drop) {
+  std::vector<Sparse1D> out(n);
+  for (int t = 0; t < n; ++t) out[t] = make_sparse(P + (int64_t)t * r * r, r, drop);
+  return out;
+}
 
 }  // namespace
 
@@ -171,20 +205,17 @@ int ttg_host_assemble_hloc(const int* r, const double* MX, const double* MY,
            sMZ = make_sparse(MZ, rz, drop);
   Sparse1D sDX = make_sparse(DX, rx, drop), sDY = make_sparse(DY, ry, drop),
            sDZ = make_sparse(DZ, rz, drop);
-  std::vector<Sparse1D> sPX(nterm), sPY(nterm), sPZ(nterm);
-  for (int t = 0; t < nterm; ++t) {
-    sPX[t] = make_sparse(PX + (int64_t)t * rx * rx, rx, drop);
-    sPY[t] = make_sparse(PY + (int64_t)t * ry * ry, ry, drop);
-    sPZ[t] = make_sparse(PZ + (int64_t)t * rz * rz, rz, drop);
-  }
+  std::vector<Sparse1D> sPX = sparse_terms(PX, nterm, rx, drop),
+                        sPY = sparse_terms(PY, nterm, ry, drop),
+                        sPZ = sparse_terms(PZ, nterm, rz, drop);
   const bool fill = (vals != nullptr);
   const double prune = truncation * 1e-6;
   RowBuilder rb{rx, ry, rz, N, &sMX, &sMY, &sMZ, &sDX, &sDY, &sDZ, &sPX, &sPY, &sPZ, nterm, coef,
-                truncation, prune};
+                nullptr, nullptr, nullptr, 0, nullptr, truncation, prune};
 
 #pragma omp parallel
   {
-    RowScratch sc(N);
+    RowScratch sc(N, false);
     std::vector<int> cols;
     std::vector<double> vs;
 #pragma omp for schedule(dynamic, 64)
@@ -207,38 +238,42 @@ int ttg_host_assemble_hloc(const int* r, const double* MX, const double* MY,
   return 0;
 }
 
-// ttg_host_assemble_hloc in one pass: every row is built once, into per-chunk
-// buffers, then copied into col_out / val_out (malloc'ed here, released with
-// ttg_host_free).  row_ptr: N + 1 entries, filled.
-int ttg_host_assemble_hloc_once(const int* r, const double* MX, const double* MY,
-                                const double* MZ, const double* DX, const double* DY,
-                                const double* DZ, int nterm, const double* coef,
-                                const double* PX, const double* PY, const double* PZ,
-                                double truncation, double drop, int64_t* row_ptr,
-                                int** col_out, double** val_out) {
-  if (!r || r[0] <= 0 || r[1] <= 0 || r[2] <= 0 || nterm < 0 || !row_ptr || !col_out ||
-      !val_out)
+}  // extern "C"
+
+namespace {
+
+// One-pass assembly: every row is built once, into per-chunk buffers, then
+// copied into col_out / val_out (malloc'ed here, released with ttg_host_free).
+int assemble_once(const int* r, const double* MX, const double* MY, const double* MZ,
+                  const double* DX, const double* DY, const double* DZ, int nterm,
+                  const double* coef, const double* PX, const double* PY, const double* PZ,
+                  int npat, const double* pcoef, const double* QX, const double* QY,
+                  const double* QZ, double truncation, double drop, int64_t* row_ptr,
+                  int** col_out, double** val_out) {
+  if (!r || r[0] <= 0 || r[1] <= 0 || r[2] <= 0 || nterm < 0 || npat < 0 || !row_ptr ||
+      !col_out || !val_out)
     return -1;
+  if (npat > 0 && (!pcoef || !QX || !QY || !QZ)) return -1;
   const int rx = r[0], ry = r[1], rz = r[2];
   const int64_t N = (int64_t)rx * ry * rz;
   Sparse1D sMX = make_sparse(MX, rx, drop), sMY = make_sparse(MY, ry, drop),
            sMZ = make_sparse(MZ, rz, drop);
   Sparse1D sDX = make_sparse(DX, rx, drop), sDY = make_sparse(DY, ry, drop),
            sDZ = make_sparse(DZ, rz, drop);
-  std::vector<Sparse1D> sPX(nterm), sPY(nterm), sPZ(nterm);
-  for (int t = 0; t < nterm; ++t) {
-    sPX[t] = make_sparse(PX + (int64_t)t * rx * rx, rx, drop);
-    sPY[t] = make_sparse(PY + (int64_t)t * ry * ry, ry, drop);
-    sPZ[t] = make_sparse(PZ + (int64_t)t * rz * rz, rz, drop);
-  }
+  std::vector<Sparse1D> sPX = sparse_terms(PX, nterm, rx, drop),
+                        sPY = sparse_terms(PY, nterm, ry, drop),
+                        sPZ = sparse_terms(PZ, nterm, rz, drop);
+  std::vector<Sparse1D> sQX = sparse_terms(QX, npat, rx, drop),
+                        sQY = sparse_terms(QY, npat, ry, drop),
+                        sQZ = sparse_terms(QZ, npat, rz, drop);
   RowBuilder rb{rx, ry, rz, N, &sMX, &sMY, &sMZ, &sDX, &sDY, &sDZ, &sPX, &sPY, &sPZ, nterm, coef,
-                truncation, truncation * 1e-6};
+                &sQX, &sQY, &sQZ, npat, pcoef, truncation, truncation * 1e-6};
   const int64_t chunk = 256, nchunks = (N + chunk - 1) / chunk;
   std::vector<std::vector<int>> ccol(nchunks);
   std::vector<std::vector<double>> cval(nchunks);
 #pragma omp parallel
   {
-    RowScratch sc(N);
+    RowScratch sc(N, npat > 0);
 #pragma omp for schedule(dynamic, 1)
     for (int64_t c = 0; c < nchunks; ++c) {
       for (int64_t I = c * chunk; I < std::min(N, (c + 1) * chunk); ++I) {
@@ -269,6 +304,40 @@ int ttg_host_assemble_hloc_once(const int* r, const double* MX, const double* MY
   *col_out = col;
   *val_out = vals;
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ttg_host_assemble_hloc in one pass (malloc'ed col_out / val_out, released
+// with ttg_host_free).  row_ptr: N + 1 entries, filled.
+int ttg_host_assemble_hloc_once(const int* r, const double* MX, const double* MY,
+                                const double* MZ, const double* DX, const double* DY,
+                                const double* DZ, int nterm, const double* coef,
+                                const double* PX, const double* PY, const double* PZ,
+                                double truncation, double drop, int64_t* row_ptr,
+                                int** col_out, double** val_out) {
+  return assemble_once(r, MX, MY, MZ, DX, DY, DZ, nterm, coef, PX, PY, PZ, 0, nullptr, nullptr,
+                       nullptr, nullptr, truncation, drop, row_ptr, col_out, val_out);
+}
+
+// As ttg_host_assemble_hloc_once, with a second CP potential (npat terms:
+// pcoef, QX, QY, QZ laid out like coef, PX, PY, PZ) that widens the pattern
+// only: an entry is kept when |h| or |h + q| exceeds the truncation, q being
+// the second potential's matrix entry, and the stored value is h.  A frozen
+// pattern built this way also holds the entries that a later potential of
+// that shape raises above the truncation.
+int ttg_host_assemble_hloc_pattern(const int* r, const double* MX, const double* MY,
+                                   const double* MZ, const double* DX, const double* DY,
+                                   const double* DZ, int nterm, const double* coef,
+                                   const double* PX, const double* PY, const double* PZ,
+                                   int npat, const double* pcoef, const double* QX,
+                                   const double* QY, const double* QZ, double truncation,
+                                   double drop, int64_t* row_ptr, int** col_out,
+                                   double** val_out) {
+  return assemble_once(r, MX, MY, MZ, DX, DY, DZ, nterm, coef, PX, PY, PZ, npat, pcoef, QX, QY,
+                       QZ, truncation, drop, row_ptr, col_out, val_out);
 }
 
 void ttg_host_free(void* p) { std::free(p); }

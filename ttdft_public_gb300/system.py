@@ -163,6 +163,12 @@ class SystemSpec:
     nonlocal_coupling: float = 0.0
     truncation: float = 1e-8
     c_truncation: float = 1e-10
+    # Pattern-only envelope (Ha; 0: off): per atom -A exp(-|r-R|^2 / (2 s^2))
+    # with s = pattern_envelope_sigma.  The frozen pattern then also keeps the
+    # entries that this potential, added to the wells, lifts above the
+    # truncation; the stored values stay the wells' operator.
+    pattern_envelope: float = 0.0
+    pattern_envelope_sigma: float = 1.6
     basis_width: float = 0.6      # Gaussian width / centre spacing of the 1-D basis
     seed: int = 1234
 
@@ -242,10 +248,12 @@ def local_potential_factors(spec: SystemSpec, atoms: np.ndarray):
     return coef
 
 
-def assemble_hloc(basis, coef, fx, fy, fz, truncation) -> tuple[Csr, dict]:
+def assemble_hloc(basis, coef, fx, fy, fz, truncation, envelope=None) -> tuple[Csr, dict]:
     """Build the 1-D matrices and call the C++ row-parallel assembly.
 
-    fx, fy, fz: (nterm, nq) CP potential factors at the quad points."""
+    fx, fy, fz: (nterm, nq) CP potential factors at the quad points.
+    envelope: None, or (coef, fx, fy, fz) of a second CP potential that widens
+    the pattern only (ttg_host_assemble_hloc_pattern)."""
     bx, by, bz = basis
     r = np.array([bx.r, by.r, bz.r], dtype=np.int32)
     MX, MY, MZ = bx.overlap(), by.overlap(), bz.overlap()
@@ -262,10 +270,22 @@ def assemble_hloc(basis, coef, fx, fy, fz, truncation) -> tuple[Csr, dict]:
     P = [np.ascontiguousarray(a, dtype=np.float64) for a in (PX, PY, PZ)]
     ptr = _lib.ptr
     cp, vp = ctypes.c_void_p(), ctypes.c_void_p()
-    rc = lib.ttg_host_assemble_hloc_once(ptr(r), *[ptr(a) for a in args], nterm, ptr(coef),
-                                         *[ptr(a) for a in P], ctypes.c_double(truncation),
-                                         ctypes.c_double(1e-15), ptr(row_ptr), ctypes.byref(cp),
-                                         ctypes.byref(vp))
+    if envelope is None:
+        rc = lib.ttg_host_assemble_hloc_once(ptr(r), *[ptr(a) for a in args], nterm, ptr(coef),
+                                             *[ptr(a) for a in P], ctypes.c_double(truncation),
+                                             ctypes.c_double(1e-15), ptr(row_ptr),
+                                             ctypes.byref(cp), ctypes.byref(vp))
+    else:
+        ecoef = np.ascontiguousarray(envelope[0], dtype=np.float64)
+        Q = [np.ascontiguousarray(np.stack([b.weighted(f[t]) for t in range(len(ecoef))]),
+                                  dtype=np.float64)
+             for b, f in zip(basis, envelope[1:])]
+        rc = lib.ttg_host_assemble_hloc_pattern(ptr(r), *[ptr(a) for a in args], nterm,
+                                                ptr(coef), *[ptr(a) for a in P], len(ecoef),
+                                                ptr(ecoef), *[ptr(a) for a in Q],
+                                                ctypes.c_double(truncation),
+                                                ctypes.c_double(1e-15), ptr(row_ptr),
+                                                ctypes.byref(cp), ctypes.byref(vp))
     if rc != 0:
         raise RuntimeError(f"H_loc assembly failed ({rc})")
     nnz = int(row_ptr[-1])
@@ -303,7 +323,9 @@ def assemble_cnloc(basis, cx, cy, cz, tol) -> Csr:
 def build_system(spec: SystemSpec, cache_dir: str | None = None) -> KSSystem:
     """Generate atoms, basis, H_loc and C for a spec (deterministic)."""
     if cache_dir:
-        path = os.path.join(cache_dir, f"{spec.name}_{spec.seed}_{spec.truncation:g}.npz")
+        env = f"_env{spec.pattern_envelope:g}_{spec.pattern_envelope_sigma:g}" \
+            if spec.pattern_envelope > 0 else ""
+        path = os.path.join(cache_dir, f"{spec.name}_{spec.seed}_{spec.truncation:g}{env}.npz")
         if os.path.exists(path):
             return _load(spec, path)
     atoms = place_atoms(spec.n_atoms, spec.box, spec.min_sep, spec.margin, spec.seed)
@@ -315,7 +337,12 @@ def build_system(spec: SystemSpec, cache_dir: str | None = None) -> KSSystem:
         fac.append(g)
         basis.append(make_basis_1d(fem, spec.rank, spec.basis_width))
     coef = -spec.z_val * np.ones(spec.n_atoms)
-    H, mats = assemble_hloc(basis, coef, fac[0], fac[1], fac[2], spec.truncation)
+    envelope = None
+    if spec.pattern_envelope > 0:
+        envelope = (-spec.pattern_envelope * np.ones(spec.n_atoms),
+                    *[np.stack([_gauss(fem.xq, atoms[a, d], spec.pattern_envelope_sigma)
+                                for a in range(spec.n_atoms)]) for d in range(3)])
+    H, mats = assemble_hloc(basis, coef, fac[0], fac[1], fac[2], spec.truncation, envelope)
     if spec.nonlocal_width > 0:
         s = spec.nonlocal_width
         norm = math.pi ** (-0.25) * s ** (-0.5)   # unit-norm 1-D Gaussian
