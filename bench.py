@@ -49,6 +49,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "s/SCF-iter & time-to-SCF @\u0394E<1e-5 Ha/atom: mixed+learned vs FP64, 1 GB300"
 WORKLOAD = "atoms512"
+PATTERN_ENVELOPE = 0.0      # Ha; > 0 widens H's frozen pattern (SystemSpec.pattern_envelope)
 MIX_ALPHA = 0.1          # Anderson mixing parameter of this workload (input parameter)
 MIX_DEPTH = 10           # Anderson history (the reference example's history=10)
 # per-workload SCF settings: the 512-atom run keeps the configuration's
@@ -167,7 +168,16 @@ def make_system():
     cache = os.environ.get("TTG_CACHE", os.path.join(ROOT, "_build", "systems"))
     if WORKLOAD == "atoms512":
         cache = None            # 14 GB of H: rebuilt rather than written to disk
-    return system.build_system(system.CONFIGS[WORKLOAD], cache_dir=cache)
+    spec = system.CONFIGS[WORKLOAD]
+    if PATTERN_ENVELOPE > 0:
+        import dataclasses
+        spec = dataclasses.replace(spec, pattern_envelope=PATTERN_ENVELOPE)
+    return system.build_system(spec, cache_dir=cache)
+
+
+def pattern_label():
+    return ("frozen at set-up from the local wells" if PATTERN_ENVELOPE <= 0 else
+            f"frozen at set-up from the wells and a {PATTERN_ENVELOPE:g} Ha envelope per atom")
 
 
 def scf_config(filt, **kw):
@@ -349,7 +359,8 @@ def run_ours(args, rank, world):
                        "l2": "inputs larger than L2: H %.2f GB on the device, %d^3 FP64 "
                              "fields of %.0f MB" % (info["device_bytes"] / 1e9,
                                                     round(nq ** (1 / 3)), nq * 8 / 1e6),
-                       "parallelism": f"replicas x{world}", "system_gen_s": round(gen_s, 1)},
+                       "parallelism": f"replicas x{world}", "system_gen_s": round(gen_s, 1),
+                       "h_pattern": pattern_label()},
             "time_to_scf": tts,
             "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": r32["achieved"], "peak": peak,
@@ -546,7 +557,8 @@ def run_reference(args, rank, world):
                 "config": {"workload": f"{WORKLOAD}: SCF iteration (FP64, host cores), {kind}",
                            "N": s.N, "states": s.spec.n_states, "degree": s.spec.degree,
                            "passes_per_iter": passes, "sampled_s": round(sampled, 1),
-                           "steps_requested": args.steps, "warmup_requested": args.warmup},
+                           "steps_requested": args.steps, "warmup_requested": args.warmup,
+                           "h_pattern": pattern_label()},
                 "cpu_baseline": {"value": v, "unit": "s/SCF-iter", "cores": oracle.threads(),
                                  "kind": "port", "sample": sample},
                 "e2e": {"value": v, "unit": "s/SCF-iter", "h2d_bytes_per_step": 0,
@@ -574,7 +586,8 @@ def run_reference(args, rank, world):
             "config": {"workload": f"{WORKLOAD}: full SCF iteration (FP64, host cores)",
                        "N": s.N, "states": s.spec.n_states, "degree": s.spec.degree,
                        "quad_points": int(np.prod(q)), "passes_per_iter": passes,
-                       "steps_requested": args.steps, "warmup_requested": args.warmup},
+                       "steps_requested": args.steps, "warmup_requested": args.warmup,
+                       "h_pattern": pattern_label()},
             "cpu_baseline": c,
             "e2e": {"value": v, "unit": "s/SCF-iter", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -593,9 +606,13 @@ def main():
     ap.add_argument("--tts", dest="tts", action="store_true", default=None,
                     help="time-to-SCF runs (default: on for atoms64, off for atoms512)")
     ap.add_argument("--no-tts", dest="tts", action="store_false")
+    ap.add_argument("--pattern-envelope", type=float, default=0.0,
+                    help="widen H's frozen pattern with a pattern-only envelope of this depth "
+                         "(Ha; 0.9 gives about the operator the reference re-truncates to)")
     args = ap.parse_args()
-    global WORKLOAD
+    global WORKLOAD, PATTERN_ENVELOPE
     WORKLOAD = args.workload
+    PATTERN_ENVELOPE = args.pattern_envelope
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
