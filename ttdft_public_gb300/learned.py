@@ -23,6 +23,7 @@ kernels of csrc/mlp.cu (forward, backward, Adam).
 
     python -m ttdft_public_gb300.learned generate --configs 40 --atoms 16 --out DATA.npz
     python -m ttdft_public_gb300.learned train --data DATA.npz [--out MODEL.npz]
+    python -m ttdft_public_gb300.learned evaluate --configs 3 --atoms 64 --seed 7001 --out EVAL.jsonl
 """
 from __future__ import annotations
 
@@ -241,6 +242,37 @@ def generate(n_configs, n_atoms, seed0, out, filt="mixed", log=print):
              n_atoms=n_atoms)
 
 
+def evaluate(n_configs, n_atoms, seed0, out, filt="mixed", log=print):
+    """Held-out check of the learned guess: on seeded configurations of
+    n_atoms at the 64-atom system's density and resolution (seeds outside
+    the training set's), one SCF from the superposition guess and one from
+    the learned guess, to the same convergence test; one JSON line per
+    configuration, written as each finishes: iterations, wall time, energies
+    and start-density errors of both runs."""
+    import json
+    from . import scf, system
+    with open(out, "a") as f:
+        for i in range(n_configs):
+            spec = training_spec(n_atoms, seed0 + i)
+            s = system.build_system(spec)
+            row = {"seed": spec.seed, "n_atoms": n_atoms, "N": s.N, "states": spec.n_states}
+            for guess in ("sad", "learned"):
+                g = scf.Scf(s, scf.ScfConfig(filter=filt, mix_alpha=0.1, history=10,
+                                             max_iter=60, guess=guess))
+                t0 = time.time()
+                res = g.run()
+                row[guess] = {"s": round(time.time() - t0, 3), "iterations": res["iterations"],
+                              "converged": bool(res["converged"]), "energy_ha": float(res["energy"]),
+                              "start_density_error": round(float(g.start_error()), 5),
+                              "guess_used": g.guess_used}
+                g.close()
+                del g
+            row["de_atom"] = abs(row["learned"]["energy_ha"] - row["sad"]["energy_ha"]) / n_atoms
+            f.write(json.dumps(row) + "\n")
+            f.flush()
+            log(json.dumps(row), flush=True)
+
+
 def train(data=DEFAULT_DATA, out=DEFAULT_MODEL, epochs=3000, batch=64, lr=2e-3,
           weight_decay=1e-3, val_frac=0.2, seed=0, chunk=50, log=print):
     """Minibatch Adam on the GPU kernels; the parameters with the lowest
@@ -304,9 +336,17 @@ def main():
     t.add_argument("--data", default=DEFAULT_DATA)
     t.add_argument("--out", default=DEFAULT_MODEL)
     t.add_argument("--epochs", type=int, default=3000)
+    e = sub.add_parser("evaluate")
+    e.add_argument("--configs", type=int, default=3)
+    e.add_argument("--atoms", type=int, default=64)
+    e.add_argument("--seed", type=int, default=7001)
+    e.add_argument("--filter", default="mixed")
+    e.add_argument("--out", required=True)
     a = ap.parse_args()
     if a.cmd == "generate":
         generate(a.configs, a.atoms, a.seed, a.out, a.filter)
+    elif a.cmd == "evaluate":
+        evaluate(a.configs, a.atoms, a.seed, a.out, a.filter)
     else:
         train(a.data, a.out, epochs=a.epochs)
 
