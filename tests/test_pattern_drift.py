@@ -103,3 +103,32 @@ def test_envelope_pattern_follows_the_retruncated_operator(drift_case):
     # measured 1.8e-8 Ha (1.7e-8 at the converged potential), against 4.4e-7
     # for the wells' pattern
     assert np.abs(w_wide - w_retrunc).max() < 5e-8
+
+
+def test_pattern_assembly_rejects_missing_envelope_arrays():
+    """npat > 0 without its coefficient or factor arrays is refused before
+    any row is built."""
+    import ctypes
+    from ttdft_public_gb300 import _lib
+    lib = _lib.host()
+    r = np.array([2, 2, 2], dtype=np.int32)
+    eye = np.ascontiguousarray(np.eye(2))
+    row_ptr = np.zeros(9, dtype=np.int64)
+    cp, vp = ctypes.c_void_p(), ctypes.c_void_p()
+    p = _lib.ptr
+    rc = lib.ttg_host_assemble_hloc_pattern(p(r), *[p(eye)] * 6, 0, None, None, None, None,
+                                            1, None, None, None, None, ctypes.c_double(1e-8),
+                                            ctypes.c_double(1e-15), p(row_ptr),
+                                            ctypes.byref(cp), ctypes.byref(vp))
+    assert rc == -1
+    # with no envelope terms it is the plain one-pass assembly; with all 1-D
+    # overlap and stiffness matrices the identity, H = 0.5 (3 I) = 1.5 I
+    rc = lib.ttg_host_assemble_hloc_pattern(p(r), *[p(eye)] * 6, 0, None, None, None, None,
+                                            0, None, None, None, None, ctypes.c_double(1e-8),
+                                            ctypes.c_double(1e-15), p(row_ptr),
+                                            ctypes.byref(cp), ctypes.byref(vp))
+    assert rc == 0 and row_ptr[-1] == 8
+    vals = np.ctypeslib.as_array(ctypes.cast(vp, ctypes.POINTER(ctypes.c_double)), (8,)).copy()
+    lib.ttg_host_free(cp)
+    lib.ttg_host_free(vp)
+    assert np.allclose(vals, 1.5)
