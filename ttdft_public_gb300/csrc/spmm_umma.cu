@@ -9,10 +9,11 @@
 // N = k states, K = 16 slots.
 //
 // Precision (FP32 degrees).  Every FP32 value v is split into three BF16 terms
-// v = v0 + v1 + v2 (|v1| <= 2^-9 |v|, |v2| <= 2^-18 |v|).  The product H Y
-// is accumulated in FP32 from the six term products of order <= 2
-// (v0w0, v0w1, v1w0, v1w1, v0w2, v2w0); the dropped ones are below 2^-26 of
-// the product, so the result carries FP32 accuracy at BF16 MMA rates.
+// v = v0 + v1 + v2 (exact for normal values; |v1| <= 2^-8 |v|,
+// |v2| <= 2^-17 |v|).  The product H Y is accumulated in FP32 from the six
+// term products of order <= 2 (v0w0, v0w1, v1w0, v1w1, v0w2, v2w0); the three
+// dropped ones are below 2^-24 of |v w| together, so the result carries FP32
+// accuracy at BF16 MMA rates.
 //
 // Data movement per chunk.
 //  - H: the three BF16 planes of the chunk (128 x 16 values each, already in
