@@ -58,15 +58,15 @@ Sparse1D make_sparse(const double* m, int r, double drop) {
 }
 
 // Scratch of one thread: a dense row accumulator, a second one for the
-// pattern-only potential (when there is one) and the list of touched columns.
+// pattern-only potential (when there is one) and a bit per column marking
+// the touched ones, scanned in column order when the row is emitted (no
+// sort), with the range of touched words.
 struct RowScratch {
   std::vector<double> row, extra;
-  std::vector<char> touched;
-  std::vector<int> touched_list;
+  std::vector<uint64_t> bits;
+  int64_t wlo, whi;
   RowScratch(int64_t n, bool with_extra)
-      : row(n, 0.0), extra(with_extra ? n : 0, 0.0), touched(n, 0) {
-    touched_list.reserve(1 << 16);
-  }
+      : row(n, 0.0), extra(with_extra ? n : 0, 0.0), bits(n / 64 + 1, 0), wlo(n), whi(-1) {}
 };
 
 // Builds one row of H_loc: the kinetic and potential Kronecker sums, then
@@ -90,13 +90,12 @@ struct RowBuilder {
            std::vector<double>& out_vals) const {
     std::vector<double>& row = s.row;
     std::vector<double>& extra = s.extra;
-    std::vector<char>& touched = s.touched;
-    std::vector<int>& touched_list = s.touched_list;
+    std::vector<uint64_t>& bits = s.bits;
     auto touch = [&](int64_t J) {
-      if (!touched[J]) {
-        touched[J] = 1;
-        touched_list.push_back((int)J);
-      }
+      const int64_t w = J >> 6;
+      bits[w] |= 1ull << (J & 63);
+      s.wlo = std::min(s.wlo, w);
+      s.whi = std::max(s.whi, w);
     };
     auto add = [&](int64_t J, double v) {
       touch(J);
@@ -152,22 +151,27 @@ struct RowBuilder {
       };
       add_cp(*sPX, *sPY, *sPZ, nterm, coef, row);
       if (npat > 0) add_cp(*sQX, *sQY, *sQZ, npat, pcoef, extra);
-      std::sort(touched_list.begin(), touched_list.end());
-      for (int J : touched_list) {
-        const double v = row[J];
-        bool keep = std::fabs(v) > truncation;
-        if (npat > 0) {
-          keep = keep || std::fabs(v + extra[J]) > truncation;
-          extra[J] = 0.0;
+      for (int64_t w = s.wlo; w <= s.whi; ++w) {
+        uint64_t word = bits[w];
+        bits[w] = 0;
+        while (word) {
+          const int J = (int)(w * 64 + __builtin_ctzll(word));
+          word &= word - 1;
+          const double v = row[J];
+          bool keep = std::fabs(v) > truncation;
+          if (npat > 0) {
+            keep = keep || std::fabs(v + extra[J]) > truncation;
+            extra[J] = 0.0;
+          }
+          if (keep) {
+            out_cols.push_back(J);
+            out_vals.push_back(v);
+          }
+          row[J] = 0.0;
         }
-        if (keep) {
-          out_cols.push_back(J);
-          out_vals.push_back(v);
-        }
-        row[J] = 0.0;
-        touched[J] = 0;
       }
-      touched_list.clear();
+      s.wlo = N;
+      s.whi = -1;
   }
 };
 
