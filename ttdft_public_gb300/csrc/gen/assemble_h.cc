@@ -97,6 +97,20 @@ struct RowBuilder {
       s.wlo = std::min(s.wlo, w);
       s.whi = std::max(s.whi, w);
     };
+    // columns J0..J1 (inclusive) at once: whole words where it can
+    auto touch_range = [&](int64_t J0, int64_t J1) {
+      const int64_t w0 = J0 >> 6, w1 = J1 >> 6;
+      const uint64_t m0 = ~0ull << (J0 & 63), m1 = ~0ull >> (63 - (J1 & 63));
+      if (w0 == w1) {
+        bits[w0] |= m0 & m1;
+      } else {
+        bits[w0] |= m0;
+        for (int64_t w = w0 + 1; w < w1; ++w) bits[w] = ~0ull;
+        bits[w1] |= m1;
+      }
+      s.wlo = std::min(s.wlo, w0);
+      s.whi = std::max(s.whi, w1);
+    };
     auto add = [&](int64_t J, double v) {
       touch(J);
       row[J] += v;
@@ -140,10 +154,16 @@ struct RowBuilder {
               const double w = wz * py.val[qy];
               if (std::fabs(w) * px.rowmax[xI] <= prune) continue;
               const int64_t base = (int64_t)rx * (yJ + (int64_t)ry * zJ);
-              for (int64_t qx = px.ptr[xI]; qx < px.ptr[xI + 1]; ++qx) {
-                const int64_t J = base + px.col[qx];
-                touch(J);
-                acc[J] += w * px.val[qx];
+              const int64_t q0 = px.ptr[xI], q1 = px.ptr[xI + 1];
+              if (q1 == q0) continue;
+              const int* cx = px.col.data();
+              const double* vx = px.val.data();
+              double* a = acc.data() + base;
+              for (int64_t qx = q0; qx < q1; ++qx) a[cx[qx]] += w * vx[qx];
+              if (cx[q1 - 1] - cx[q0] == q1 - 1 - q0) {
+                touch_range(base + cx[q0], base + cx[q1 - 1]);
+              } else {
+                for (int64_t qx = q0; qx < q1; ++qx) touch(base + cx[qx]);
               }
             }
           }
