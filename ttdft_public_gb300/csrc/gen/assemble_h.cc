@@ -157,13 +157,18 @@ struct RowBuilder {
               const int64_t q0 = px.ptr[xI], q1 = px.ptr[xI + 1];
               if (q1 == q0) continue;
               const int* cx = px.col.data();
-              const double* vx = px.val.data();
-              double* a = acc.data() + base;
-              for (int64_t qx = q0; qx < q1; ++qx) a[cx[qx]] += w * vx[qx];
-              if (cx[q1 - 1] - cx[q0] == q1 - 1 - q0) {
+              const double* __restrict__ vx = px.val.data() + q0;
+              const int64_t n = q1 - q0;
+              if (cx[q1 - 1] - cx[q0] == n - 1) {          // a run of columns: axpy
+                double* __restrict__ a = acc.data() + base + cx[q0];
+                for (int64_t i = 0; i < n; ++i) a[i] += w * vx[i];
                 touch_range(base + cx[q0], base + cx[q1 - 1]);
               } else {
-                for (int64_t qx = q0; qx < q1; ++qx) touch(base + cx[qx]);
+                double* a = acc.data() + base;
+                for (int64_t i = 0; i < n; ++i) {
+                  a[cx[q0 + i]] += w * vx[i];
+                  touch(base + cx[q0 + i]);
+                }
               }
             }
           }
