@@ -15,6 +15,7 @@ under tests/golden/, and by invariants.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import subprocess
 
@@ -195,6 +196,44 @@ def expansion_factor(alpha, x, xq, wq, U):
     """F_t[i, a] = sum_q wq exp(-alpha_t (x_i - xq)^2) U[q, a]  (KSDFTPotential.cc:509-523)."""
     E = np.exp(-alpha[:, None, None] * (x[None, :, None] - xq[None, None, :]) ** 2)
     return np.einsum("tiq,q,qa->tia", E, wq, U, optimize=True)
+
+
+def expansion_kernel_exact(alpha, x, edges, xq):
+    """The factor integrals of KSDFTPotential.cc:509-523 without quadrature
+    error: K_t[i, q] such that sum_q K_t[i, q] U[q, a] is
+    int exp(-alpha_t (x_i - y)^2) u_a(y) dy exactly, u_a the quadratic through
+    U's values at each element's three quadrature points (product
+    integration: per element the moments int t^k exp(-alpha t^2) dt, k <= 2,
+    in closed form with erf).  expansion_factor's sum, by contrast, samples
+    exp(-alpha_t (x_i - y)^2) at the quadrature points, which the narrow terms
+    of the expansion (widths down to 5e-3 bohr) do not resolve.
+    Returns (t, len(x), len(xq))."""
+    import scipy.special
+    alpha = np.asarray(alpha, np.float64)
+    n_el = edges.size - 1
+    mid = 0.5 * (edges[:-1] + edges[1:])
+    se = xq.reshape(n_el, 3) - mid[:, None]          # quadrature points about the element centre
+    # coefficients of the quadratic in s = y - mid_e through the three points
+    Vinv = np.linalg.inv(np.stack([np.ones_like(se), se, se ** 2], axis=2))   # (e, k, q)
+    ta = edges[None, :-1] - x[:, None]                                          # (i, e): t = y - x_i
+    tb = edges[None, 1:] - x[:, None]
+    xi = x[:, None] - mid[None, :]                                              # s = t + xi
+    K = np.zeros((alpha.size, x.size, xq.size))
+    for t, al in enumerate(alpha):
+        ea, eb = np.exp(-al * ta * ta), np.exp(-al * tb * tb)
+        sa = math.sqrt(al)
+        I0 = 0.5 * math.sqrt(math.pi / al) * (scipy.special.erf(sa * tb)
+                                              - scipy.special.erf(sa * ta))
+        I1 = -(eb - ea) / (2.0 * al)
+        I2 = I0 / (2.0 * al) - (tb * eb - ta * ea) / (2.0 * al)
+        # moments of s^k over the element, s = t + (x_i - mid_e)
+        M0 = I0
+        M1 = xi * I0 + I1
+        M2 = xi * xi * I0 + 2.0 * xi * I1 + I2
+        Kt = (np.einsum("ie,eq->ieq", M0, Vinv[:, 0, :]) + np.einsum("ie,eq->ieq", M1, Vinv[:, 1, :])
+              + np.einsum("ie,eq->ieq", M2, Vinv[:, 2, :]))
+        K[t] = Kt.reshape(x.size, xq.size)
+    return K
 
 
 def hartree(alpha, omega, G, quad, Uq, grids):

@@ -95,3 +95,35 @@ def test_linear_in_the_charge():
     p1, _ = poisson.solve_hartree(rho, edges, [[3.0, 5.0, 5.0, 5.0]], n_outer=8)
     p2, _ = poisson.solve_hartree(2.0 * rho, edges, [[6.0, 5.0, 5.0, 5.0]], n_outer=8)
     assert np.abs(p2 - 2.0 * p1).max() < 1e-8 * np.abs(p2).max()
+
+
+def test_exact_factor_integrals_remove_the_quadrature_error():
+    """oracle.expansion_kernel_exact: the factor integrals by product
+    integration (closed-form moments of each element's quadratic against
+    exp(-alpha t^2)).  Along the line through a unit-width Gaussian charge on
+    the 64-atom system's mesh (120 elements on 32 bohr): relative L2 error
+    1.5e-6 against 7.2e-2 for the quadrature sums; and the kernel reproduces
+    the quadrature sums exactly for quadratics, where both are exact."""
+    alpha, omega = coulomb_expansion()
+    fem = system.Fem1D(120, 0.0, 32.0)
+    xq, edges = fem.xq, np.linspace(0.0, 32.0, 121)
+    K = oracle.expansion_kernel_exact(alpha, xq, edges, xq)
+    c, Q = 7.3, 3.0
+    g = np.exp(-(xq - c) ** 2)
+    j = np.argmin(np.abs(xq - c))
+    r = np.sqrt((xq - c) ** 2 + 2 * (xq[j] - c) ** 2)
+    exact = Q * scipy.special.erf(r) / r
+    errs = {}
+    for name, F in (("exact", np.einsum("tiq,q->ti", K, g)),
+                    ("quadrature", oracle.expansion_factor(alpha, xq, xq, fem.wJ,
+                                                           g[:, None])[:, :, 0])):
+        V = Q / np.pi ** 1.5 * np.einsum("t,ti,t,t->i", omega, F, F[:, j], F[:, j])
+        errs[name] = np.linalg.norm(V - exact) / np.linalg.norm(exact)
+    assert errs["exact"] < 1e-5 and errs["quadrature"] > 1e-2
+    # the widest terms (alpha -> 0): the kernel integrates a quadratic exactly,
+    # as the 3-point rule does
+    U = np.stack([np.ones_like(xq), xq, xq ** 2], axis=1)
+    small = np.array([1e-9])
+    Ke = oracle.expansion_kernel_exact(small, xq, edges, xq)[0] @ U
+    Kq = oracle.expansion_factor(small, xq, xq, fem.wJ, U)[0]
+    assert np.abs(Ke - Kq).max() < 1e-6 * np.abs(Kq).max()
