@@ -356,7 +356,8 @@ def run_ours(args, rank, world):
                        "mix_alpha": mix_alpha,
                        "nnz_per_row": info["nnz_h"] / n, "nproj": s.C.n_rows,
                        "passes_per_iter": passes, "iters_timed": [r["iter"] for r in recs],
-                       "l2": "inputs larger than L2: H %.2f GB on the device, %d^3 FP64 "
+                       "l2": "inputs larger than L2: the operator (H in its formats, the "
+                             "block and its scratch) %.2f GB on the device, %d^3 FP64 "
                              "fields of %.0f MB" % (info["device_bytes"] / 1e9,
                                                     round(nq ** (1 / 3)), nq * 8 / 1e6),
                        "parallelism": f"replicas x{world}", "system_gen_s": round(gen_s, 1),
