@@ -236,11 +236,15 @@ def expansion_kernel_exact(alpha, x, edges, xq):
     return K
 
 
-def hartree(alpha, omega, G, quad, Uq, grids):
+def hartree(alpha, omega, G, quad, Uq, grids, kernels=None):
     """V = sum_t omega_t G x1 Fx_t x2 Fy_t x3 Fz_t (KSDFTPotential.cc:269-340, 601-658).
-    G as (rz, ry, rx); returns (nz, ny, nx)."""
+    G as (rz, ry, rx); returns (nz, ny, nx).  kernels: optional per-direction
+    K_t (expansion_kernel_exact) in place of the quadrature sums."""
     alpha = np.asarray(alpha, np.float64)
-    F = [expansion_factor(alpha, grids[d], quad[d][0], quad[d][1], Uq[d]) for d in range(3)]
+    if kernels is None:
+        F = [expansion_factor(alpha, grids[d], quad[d][0], quad[d][1], Uq[d]) for d in range(3)]
+    else:
+        F = [np.einsum("tiq,qa->tia", kernels[d], Uq[d], optimize=True) for d in range(3)]
     V = np.zeros((grids[2].size, grids[1].size, grids[0].size))
     for t in range(alpha.size):
         V += omega[t] * np.einsum("cba,ia,jb,lc->lji", G, F[0][t], F[1][t], F[2][t], optimize=True)

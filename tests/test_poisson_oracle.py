@@ -127,3 +127,27 @@ def test_exact_factor_integrals_remove_the_quadrature_error():
     Ke = oracle.expansion_kernel_exact(small, xq, edges, xq)[0] @ U
     Kq = oracle.expansion_factor(small, xq, xq, fem.wJ, U)[0]
     assert np.abs(Ke - Kq).max() < 1e-6 * np.abs(Kq).max()
+
+
+def test_oracle_hartree_contraction_against_closed_form():
+    """The oracle's Tucker contraction of the expansion (the checker of the
+    device Hartree), fed exact factor integrals, reproduces the closed-form
+    potential of the 2-atom superposition density on the full 3-D grid: a
+    known answer for its axis order, weights and term sum (measured 6.2e-5
+    relative L2; the quadrature sums on this 0.625-bohr mesh: 0.13)."""
+    spec = system.small_spec(n_el=16, rank=8)
+    s = system.build_system(spec)
+    grids = [b.fem.xq for b in s.basis]
+    rho = oracle.sad_density(s.atoms, grids, spec.z_val, 1.0)
+    alpha, omega = coulomb_expansion()
+    quad = [(b.fem.xq, b.fem.wJ) for b in s.basis]
+    K = [oracle.expansion_kernel_exact(alpha, g, np.linspace(b.fem.x0, b.fem.x1, b.fem.n_el + 1), g)
+         for g, b in zip(grids, s.basis)]
+    U = [np.eye(g.size) for g in grids]
+    V = oracle.hartree(alpha, omega, rho, quad, U, grids, kernels=K)
+    Z, Y, X = np.meshgrid(grids[2], grids[1], grids[0], indexing="ij")
+    exact = np.zeros_like(rho)
+    for a in s.atoms:
+        r = np.sqrt((X - a[0]) ** 2 + (Y - a[1]) ** 2 + (Z - a[2]) ** 2)
+        exact += spec.z_val * scipy.special.erf(r) / r
+    assert np.linalg.norm(V - exact) / np.linalg.norm(exact) < 1e-4
